@@ -1,0 +1,286 @@
+/*
+ * msbfs.h -- C ABI of the GB300 multi-source BFS engine (libmsbfs.so).
+ *
+ * This is the drop-in boundary for the reference's GPU multi-source BFS path
+ * (crates/gpu_bfs, likr-sandbox/webgpu-bfs). Every entry point below names
+ * the reference interface it replaces (file:line inside that project). The
+ * signatures carry plain pointers and sizes only: no CUDA, PyTorch or C++
+ * types cross the boundary, so a Rust `extern "C"` block, ctypes or any other
+ * FFI can bind it.
+ *
+ * Result contract (crates/core/src/lib.rs:21-39): distances are u32 hop
+ * counts laid out source-major, dist[s * V + v]; dist[s * V + sources[s]] = 0;
+ * unreachable = 0xFFFFFFFF. Duplicate sources are allowed and each gets its
+ * own row. Every correct BFS produces identical bytes, so every method below
+ * returns the same output for the same graph and sources.
+ *
+ * Threading: an engine serialises its own calls with an internal mutex (the
+ * reference locks one Mutex per pooled method, crates/gpu_bfs/src/engine.rs:
+ * 259-281). Distinct engines may be used from distinct threads.
+ */
+#ifndef MSBFS_H
+#define MSBFS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSBFS_ABI_VERSION 1
+
+/* ---- status codes (the reference returns anyhow::Error strings) ---------- */
+#define MSBFS_OK 0
+/* "Source vertex {} at index {} exceeds graph vertex count {}"
+ * (crates/gpu_bfs/src/engine.rs:240-248). */
+#define MSBFS_ERR_SOURCE_OOB 1
+/* V == 0 with S > 0 (engine.rs:233-238). */
+#define MSBFS_ERR_EMPTY_GRAPH 2
+#define MSBFS_ERR_OOM 3
+/* A bounded device-side loop ran out of iterations (reported, never hung). */
+#define MSBFS_ERR_TIMEOUT 4
+#define MSBFS_ERR_CUDA 5
+/* CsrGraph::validate failed (crates/core/src/graph.rs:226-280). */
+#define MSBFS_ERR_INVALID_GRAPH 6
+#define MSBFS_ERR_INVALID_ARGUMENT 7
+#define MSBFS_ERR_NO_DEVICE 8
+
+/* ---- methods: same names and order as GpuBfsMethod (engine.rs:33-53) ------
+ * Every method produces identical bytes. On GB300 they map onto four kernel
+ * paths: level-synchronous bit-parallel push, pull or device-switched hybrid,
+ * and the CTA-per-source persistent BFS. */
+typedef enum msbfs_method {
+  MSBFS_METHOD_NAIVE_SEQUENTIAL = 0,
+  MSBFS_METHOD_BATCHED_DENSE_SPMM = 1,
+  MSBFS_METHOD_BIT_PARALLEL_32 = 2,
+  MSBFS_METHOD_BIT_PARALLEL_64 = 3,
+  MSBFS_METHOD_BIT_PARALLEL_64_PULL = 4,
+  MSBFS_METHOD_BOOLEAN_REACHABILITY = 5,
+  MSBFS_METHOD_PUSH_PULL_ADAPTIVE = 6,
+  MSBFS_METHOD_SPARSE_QUEUE = 7,
+  MSBFS_METHOD_SPARSE_BIT_PARALLEL_64 = 8,
+  MSBFS_METHOD_MULTI_WORD_BIT_PARALLEL = 9,
+  MSBFS_METHOD_INDIRECT_MACRO_BATCH = 10,
+  MSBFS_METHOD_INDIRECT_SPARSE_QUEUE_PUSH = 11,
+  MSBFS_METHOD_MULTI_WORD_BIT_PARALLEL_PUSH = 12,
+  MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS = 13,
+  MSBFS_METHOD_AUTO = 14
+} msbfs_method;
+
+/* Kernel path a call actually ran (reported in msbfs_stats.path). */
+#define MSBFS_PATH_NONE 0
+#define MSBFS_PATH_PUSH 1   /* level-synchronous, top-down only            */
+#define MSBFS_PATH_PULL 2   /* level-synchronous, bottom-up only           */
+#define MSBFS_PATH_HYBRID 3 /* level-synchronous, device-decided direction */
+#define MSBFS_PATH_CTA 4    /* one CTA per source, whole BFS in one launch */
+
+typedef struct msbfs_engine msbfs_engine;
+typedef struct msbfs_graph msbfs_graph;
+
+/* Per-call statistics (filled when a non-NULL pointer is passed). */
+typedef struct msbfs_stats {
+  uint32_t method;           /* resolved msbfs_method                        */
+  uint32_t path;             /* MSBFS_PATH_*                                 */
+  uint32_t passes;           /* source chunks traversed                      */
+  uint32_t words_per_vertex; /* u32 frontier words per vertex per pass       */
+  uint32_t levels;           /* max BFS levels over passes                   */
+  uint32_t push_levels;      /* summed over passes                           */
+  uint32_t pull_levels;      /* summed over passes                           */
+  uint32_t reserved0;
+  uint64_t reached_pairs;    /* (s, v) pairs with a finite distance          */
+  double gpu_ms;             /* device time of the whole call (CUDA events)  */
+} msbfs_stats;
+
+/* One record per launch of the level kernel (and one for the distance
+ * materialisation), collected when profiling is on. Counters are those the
+ * kernels keep for the algorithmic-bytes model; no reference counterpart
+ * (the wgpu path has no timestamp queries, multi_word_bp.rs:762). */
+#define MSBFS_DIR_TOP_DOWN 0
+#define MSBFS_DIR_BOTTOM_UP 1
+#define MSBFS_DIR_MATERIALIZE 2
+typedef struct msbfs_level_record {
+  uint32_t pass;
+  uint32_t level;
+  uint32_t dir;               /* MSBFS_DIR_*                               */
+  uint32_t frontier_vertices; /* vertices in the level's input frontier    */
+  uint64_t frontier_entries;  /* queue entries (hubs split into slices)    */
+  uint64_t active;            /* bottom-up: vertex rows read               */
+  uint64_t edges;             /* bottom-up: in-neighbour gathers;
+                                 top-down: out-edges walked                */
+  uint64_t new_vertices;      /* vertices that gained a visited lane       */
+  uint64_t new_pairs;         /* (source, vertex) pairs discovered         */
+  double device_ms;           /* %globaltimer span of the launch           */
+  double event_ms;            /* CUDA-event span (profiling level 2) or 0  */
+} msbfs_level_record;
+
+/* Host-side CSR, mirroring CsrGraph (crates/core/src/graph.rs:8-22):
+ * row_offsets[V+1], col_indices[E], u32, sorted and deduplicated rows.
+ * Arrays returned by the library are malloc'd; release them with
+ * msbfs_csr_free. The same struct carries a CscGraph (graph.rs:27-41) with
+ * row_offsets = col_offsets and col_indices = row_indices. */
+typedef struct msbfs_csr {
+  size_t num_vertices;
+  size_t num_edges;
+  uint32_t *row_offsets;
+  uint32_t *col_indices;
+} msbfs_csr;
+
+/* ======================= engine (crates/gpu_bfs) ========================== */
+
+/* GpuBfsEngine::new (engine.rs:68-78): binds CUDA device `device` and fixes
+ * the default method. */
+int msbfs_engine_create(int device, int method, msbfs_engine **out);
+void msbfs_engine_destroy(msbfs_engine *engine);
+/* GpuBfsEngine::method (engine.rs:209-212). */
+int msbfs_engine_method(const msbfs_engine *engine);
+/* Text of the last error on this engine (anyhow message in the reference). */
+const char *msbfs_engine_last_error(const msbfs_engine *engine);
+/* Launch on a caller-owned cudaStream_t (NULL = the engine's own stream).
+ * No reference counterpart: wgpu owns its queue. */
+int msbfs_engine_set_stream(msbfs_engine *engine, void *cuda_stream);
+/* Tuning knobs of the level-synchronous path (no reference counterpart; the
+ * reference hard-codes alpha=14/beta=24 in push_pull.rs:29-36 and 512-source
+ * chunks in multi_word_bp.rs:630). Zero keeps the current value. */
+int msbfs_engine_set_tuning(msbfs_engine *engine, uint32_t max_words_per_pass,
+                            uint32_t alpha, uint32_t beta);
+
+/* Profiling: 0 off; 1 keep a per-level record of every call (device timers,
+ * the level loop stays on the device); 2 as 1, but the level loop is driven
+ * from the host one launch at a time with CUDA events around each launch.
+ * msbfs_engine_level_log copies the last call's records. */
+int msbfs_engine_set_profiling(msbfs_engine *engine, int level);
+int msbfs_engine_level_log(const msbfs_engine *engine, msbfs_level_record *out,
+                           size_t capacity, size_t *count);
+
+/* GpuBfsEngine::select_auto_method (engine.rs:157-198), same branches:
+ * empty graph or S == 0 -> NAIVE_SEQUENTIAL; max_degree <= 8 && E <= 4V ->
+ * WORKGROUP_PERSISTENT_BFS; max_degree >= 128 -> INDIRECT_SPARSE_QUEUE_PUSH;
+ * else S >= 64 -> MULTI_WORD_BIT_PARALLEL, S >= 32 -> BIT_PARALLEL_64,
+ * S > 1 -> BIT_PARALLEL_32, S == 1 -> SPARSE_QUEUE. */
+int msbfs_select_auto_method(size_t num_vertices, size_t num_edges,
+                             const uint32_t *row_offsets, size_t num_sources);
+
+/* Uploads a CsrGraph and keeps it resident in HBM: CSR for top-down steps
+ * and its transpose (CSC) for bottom-up steps, aliased when the graph is
+ * symmetric (PushPullGraphBuffers::from_symmetric_graph / from_graph,
+ * crates/gpu_bfs/src/buffer.rs:108-221). The arrays are validated like
+ * CsrGraph::validate (graph.rs:226-280) and copied; the caller keeps
+ * ownership. */
+int msbfs_graph_create(msbfs_engine *engine, size_t num_vertices,
+                       size_t num_edges, const uint32_t *row_offsets,
+                       const uint32_t *col_indices, msbfs_graph **out);
+void msbfs_graph_destroy(msbfs_graph *graph);
+/* Graph facts used by the router: V, E, max out-degree, symmetric flag. */
+int msbfs_graph_info(const msbfs_graph *graph, size_t *num_vertices,
+                     size_t *num_edges, uint32_t *max_degree,
+                     int *is_symmetric);
+
+/* BfsEngine::run_ms_bfs / GpuBfsEngine::run_ms_bfs_into (crates/core/src/
+ * lib.rs:38, engine.rs:219-298) with the engine's method (AUTO resolves per
+ * call). `out` is caller-owned HOST memory of S*V u32. S == 0 writes nothing
+ * and succeeds; V == 0 with S > 0 is MSBFS_ERR_EMPTY_GRAPH; a source >= V is
+ * MSBFS_ERR_SOURCE_OOB and nothing is written. Blocks until `out` is filled. */
+int msbfs_run_ms_bfs(msbfs_engine *engine, const msbfs_graph *graph,
+                     const uint32_t *sources, size_t num_sources,
+                     uint32_t *out, msbfs_stats *stats);
+
+/* GpuBfsEngine::run_ms_bfs_with_method (engine.rs:300-405). */
+int msbfs_run_ms_bfs_with_method(msbfs_engine *engine, int method,
+                                 const msbfs_graph *graph,
+                                 const uint32_t *sources, size_t num_sources,
+                                 uint32_t *out, msbfs_stats *stats);
+
+/* One-shot form of BfsEngine::run_ms_bfs(&CsrGraph, &[u32]) for callers that
+ * hold only host CSR arrays: uploads the graph for this call, runs, frees. */
+int msbfs_run_ms_bfs_csr(msbfs_engine *engine, size_t num_vertices,
+                         size_t num_edges, const uint32_t *row_offsets,
+                         const uint32_t *col_indices, const uint32_t *sources,
+                         size_t num_sources, uint32_t *out, msbfs_stats *stats);
+
+/* Device-resident form of run_ms_bfs_into: `out_device` is a device pointer
+ * to S*V u32. Work is queued on the engine's stream and the call returns
+ * without waiting; msbfs_engine_synchronize waits and fills `stats`. Sources
+ * are validated on the host before anything is queued. No reference
+ * counterpart (the wgpu path always reads back to the host). */
+int msbfs_run_ms_bfs_device(msbfs_engine *engine, int method,
+                            const msbfs_graph *graph, const uint32_t *sources,
+                            size_t num_sources, uint32_t *out_device);
+int msbfs_engine_synchronize(msbfs_engine *engine, msbfs_stats *stats);
+
+/* GpuBfsEngine::run_ms_reachability (engine.rs:420-479): HOST words of
+ * V * ceil(S/32) u32, words[v * wpv + s / 32] bit (s % 32) set iff v is
+ * reachable from sources[s] (ReachabilityBitmask, graph.rs:446-452). */
+int msbfs_run_reachability(msbfs_engine *engine, const msbfs_graph *graph,
+                           const uint32_t *sources, size_t num_sources,
+                           uint32_t *words, msbfs_stats *stats);
+
+/* Traversed edges of a result, sum over s of out-degrees of reached vertices
+ * (crates/cli/src/bench.rs:478-491), computed on the device from a
+ * device-resident distance matrix. */
+int msbfs_traversed_edges_device(msbfs_engine *engine, const msbfs_graph *graph,
+                                 const uint32_t *dist_device,
+                                 size_t num_sources, uint64_t *out_edges);
+
+/* ===================== graph core (crates/core) =========================== */
+
+void msbfs_csr_free(msbfs_csr *csr);
+/* CsrGraph::from_edge_list (graph.rs:51-79): drops self-loops and
+ * out-of-range endpoints, sorts by (u, v) and deduplicates. */
+int msbfs_csr_from_edge_list(size_t num_vertices, size_t num_pairs,
+                             const uint32_t *src, const uint32_t *dst,
+                             msbfs_csr *out);
+/* CsrGraph::to_csc (graph.rs:90-127); also CscGraph::to_csr (graph.rs:
+ * 283-316), which is the same counting-sort transpose. */
+int msbfs_csr_transpose(const msbfs_csr *in, msbfs_csr *out);
+/* CsrGraph::is_symmetric (graph.rs:129-133): 1 / 0. */
+int msbfs_csr_is_symmetric(const msbfs_csr *csr);
+/* CsrGraph::to_undirected (graph.rs:136-151). */
+int msbfs_csr_to_undirected(const msbfs_csr *in, msbfs_csr *out);
+/* CsrGraph::validate (graph.rs:226-280); message written to `msg`. */
+int msbfs_csr_validate(const msbfs_csr *csr, char *msg, size_t msg_len);
+/* CsrGraph::max_degree (graph.rs:209-214). */
+uint32_t msbfs_csr_max_degree(const msbfs_csr *csr);
+
+/* ==================== generators (crates/core/src/generators.rs) ==========
+ * Seeded with the engine's own counter-based generator (splitmix64), so the
+ * bytes differ from the reference's rand::StdRng for the same seed; the
+ * structural rules (symmetrised, sorted, deduplicated, no self-loops) are the
+ * reference's. */
+/* Grid2D::new (generators.rs:28-80): N, W, E, S neighbour order. */
+int msbfs_gen_grid2d(size_t width, size_t height, msbfs_csr *out);
+/* generate_erdos_renyi_np (generators.rs:139-191), geometric skipping. */
+int msbfs_gen_erdos_renyi_np(size_t n, double p, uint64_t seed, msbfs_csr *out);
+/* generate_random_tree (generators.rs:239-262): uniform recursive tree over
+ * a shuffled vertex order. */
+int msbfs_gen_random_tree(size_t n, uint64_t seed, msbfs_csr *out);
+/* generate_rmat (generators.rs:277-342): quadrant recursion, self-loops
+ * dropped, symmetrised unless `directed`. Multi-threaded; the output does not
+ * depend on the thread count. */
+int msbfs_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
+                   double c, double d, uint64_t seed, int directed,
+                   msbfs_csr *out);
+/* path_graph, star_graph, cycle_graph, clique_graph, disconnected_cliques
+ * (generators.rs:388-544). */
+int msbfs_gen_path(size_t n, msbfs_csr *out);
+int msbfs_gen_star(size_t n, msbfs_csr *out);
+int msbfs_gen_cycle(size_t n, msbfs_csr *out);
+int msbfs_gen_clique(size_t n, msbfs_csr *out);
+int msbfs_gen_disconnected_cliques(const size_t *sizes, size_t count,
+                                   msbfs_csr *out);
+/* Road-like graph (no reference counterpart): a uniform spanning tree of the
+ * width x height 4-neighbour grid drawn with Wilson's algorithm, plus
+ * `extra_edges` distinct grid edges not in the tree, symmetrised. */
+int msbfs_gen_wilson_grid(size_t width, size_t height, size_t extra_edges,
+                          uint64_t seed, msbfs_csr *out);
+/* sample_sources, random strategy (crates/cli/src/graph_loader.rs:132-190):
+ * `count` distinct vertices drawn uniformly without replacement among those
+ * with out-degree >= min_degree, returned sorted ascending. */
+int msbfs_sample_sources(const msbfs_csr *csr, size_t count, uint64_t seed,
+                         uint32_t min_degree, uint32_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSBFS_H */

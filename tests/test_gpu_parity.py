@@ -1,0 +1,197 @@
+"""Bit-exact parity of the sm_103a engine with the CPU oracle (GPU).
+
+Mirrors the reference's GPU suites: golden known answers for every kernel
+path (tests/common/oracles.rs), batch sizes straddling word boundaries
+(tests/tier2_boundaries/b6_batch_sizes.rs), directed graphs
+(tests/tier3_combinations/t3_03_asymmetric_pushpull.rs), duplicate sources,
+pooled-buffer re-entrancy (crates/gpu_bfs/tests/m19_adversarial_challenge.rs)
+and error behaviour (crates/gpu_bfs/src/engine.rs:228-248). Tolerance: none,
+every u32 must match.
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_same, case_graph
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ["Auto", "PushPullAdaptive", "MultiWordBitParallel", "BitParallel64",
+           "WorkgroupPersistentBfs", "SparseQueue", "IndirectSparseQueuePush"]
+
+
+def _oracle(oracle, g, src):
+    return oracle.ms_bfs_fifo(g.num_vertices, g.row_offsets, g.col_indices, src)
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_golden_cases(native, gpu_engine, golden, method):
+    m = native.GpuBfsMethod[method]
+    for case in golden["bfs"]:
+        g = case_graph(native, case)
+        got = gpu_engine.run_ms_bfs_with_method(m, g, case["sources"])
+        assert_same(got, case["dist"], g, case["sources"], f"{case['name']}/{method}")
+
+
+def _graphs(native):
+    return {
+        "er": native.generate_erdos_renyi_np(3000, 8 / 2999, 1),
+        "rmat12": native.generate_graph500_rmat(12, 16, 2),
+        "rmat12_directed": native.generate_rmat(12, 8, 0.57, 0.19, 0.19, 0.05, 3, directed=True),
+        "tree": native.generate_random_tree(2000, 4),
+        "wilson": native.wilson_grid(60, 50, 80, 5),
+        "grid64": native.generate_grid2d(64, 64),
+    }
+
+
+@pytest.mark.parametrize("S", [1, 3, 17, 31, 33, 63, 65, 129, 512, 700, 2048])
+def test_batch_sizes_all_paths(native, gpu_engine, oracle, S):
+    rng = np.random.default_rng(S)
+    for name, g in _graphs(native).items():
+        src = rng.integers(0, g.num_vertices, S).astype(np.uint32)
+        want = _oracle(oracle, g, src)
+        for method in ("Auto", "PushPullAdaptive", "MultiWordBitParallel", "BitParallel64",
+                       "WorkgroupPersistentBfs"):
+            got = gpu_engine.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, src)
+            assert_same(got, want, g, src, f"{name}/S={S}/{method}")
+
+
+@pytest.mark.parametrize("max_words", [1, 2, 4, 8, 16, 32, 64])
+def test_every_word_width(native, oracle, max_words):
+    """Passes of 32*W sources for every compiled W, several passes per call."""
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.PushPullAdaptive)
+    try:
+        eng.set_tuning(max_words_per_pass=max_words)
+        g = native.generate_graph500_rmat(11, 8, 11)
+        S = 32 * max_words * 2 + 5
+        src = np.random.default_rng(max_words).integers(0, g.num_vertices, S).astype(np.uint32)
+        want = _oracle(oracle, g, src)
+        for method in ("PushPullAdaptive", "MultiWordBitParallel", "BitParallel64"):
+            got = eng.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, src)
+            assert_same(got, want, g, src, f"W={max_words}/{method}")
+        assert eng.last_stats["words_per_vertex"] == max_words
+        assert eng.last_stats["passes"] == 3
+    finally:
+        eng.close()
+
+
+def test_deep_levels_beyond_level_planes(native, gpu_engine, oracle):
+    """Distances >= 256 are written directly (beyond the 8 bit-planes)."""
+    g = native.path_graph(1500)
+    src = np.array([0, 1499, 700, 3], np.uint32)
+    want = _oracle(oracle, g, src)
+    for method in ("PushPullAdaptive", "MultiWordBitParallel", "BitParallel64",
+                   "WorkgroupPersistentBfs"):
+        got = gpu_engine.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, src)
+        assert_same(got, want, g, src, f"path1500/{method}")
+
+
+def test_duplicate_sources_and_isolated(native, gpu_engine, oracle):
+    g = native.generate_graph500_rmat(10, 4, 21)
+    src = np.array([5, 5, 5, 0, 1023, 5] + list(range(40)), np.uint32)
+    want = _oracle(oracle, g, src)
+    for method in METHODS:
+        got = gpu_engine.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, src)
+        assert_same(got, want, g, src, f"dups/{method}")
+
+
+def test_directed_dag_row(native, gpu_engine, golden):
+    case = next(c for c in golden["bfs"] if c["name"] == "dag_50_source_49")
+    g = case_graph(native, case)
+    src = [0, 10, 20, 30, 40, 49]
+    from oracle import oracle as o
+    want = o.ms_bfs_fifo(50, g.row_offsets, g.col_indices, src)
+    for method in METHODS:
+        got = gpu_engine.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, src)
+        assert_same(got, want, g, src, f"dag/{method}")
+        row = got[5 * 50:6 * 50]
+        assert row[49] == 0 and np.all(row[:49] == 0xFFFFFFFF)
+
+
+def test_errors_match_reference(native, gpu_engine):
+    g = native.path_graph(5)
+    with pytest.raises(native.BfsError) as ei:
+        gpu_engine.run_ms_bfs(g, [1, 2, 7])
+    assert ei.value.code == 1
+    assert str(ei.value) == "Source vertex 7 at index 2 exceeds graph vertex count 5"
+    with pytest.raises(native.BfsError) as ei:
+        gpu_engine.run_ms_bfs(native.empty_graph(), [0])
+    assert ei.value.code == 2
+    assert gpu_engine.run_ms_bfs(g, []).size == 0
+    assert gpu_engine.run_ms_bfs(native.empty_graph(), []).size == 0
+    m = gpu_engine.run_ms_reachability(native.empty_graph(), [])
+    assert m.words.size == 0
+
+
+def test_pooled_reentrancy_same_shape_graphs(native, gpu_engine, oracle):
+    """Two different graphs with identical (V, E) must not share stale state
+    (the reference keys its pool on (V, E) only)."""
+    a = native.generate_grid2d(40, 40)
+    b_edges = [(u, int(v)) for u in range(a.num_vertices)
+               for v in a.neighbors((u * 7) % a.num_vertices)]
+    b = native.CsrGraph.from_edge_list(a.num_vertices, b_edges)
+    src = np.arange(0, 1600, 9, dtype=np.uint32)
+    for g in (a, b, a, b):
+        for method in ("PushPullAdaptive", "WorkgroupPersistentBfs"):
+            got = gpu_engine.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, src)
+            assert_same(got, _oracle(oracle, g, src), g, src, f"reentrant/{method}")
+
+
+def test_reachability(native, gpu_engine, oracle):
+    for g, S in ((native.generate_graph500_rmat(11, 8, 31), 700),
+                 (native.wilson_grid(30, 30, 20, 2), 65),
+                 (native.generate_rmat(10, 8, 0.57, 0.19, 0.19, 0.05, 6, directed=True), 33)):
+        src = np.random.default_rng(S).integers(0, g.num_vertices, S).astype(np.uint32)
+        dist = _oracle(oracle, g, src)
+        want = oracle.reachability_from_distances(g.num_vertices, S, dist)
+        got = gpu_engine.run_ms_reachability(g, src)
+        assert got.words_per_vertex == (S + 31) // 32
+        assert_same(got.words, want, label=f"reach/V={g.num_vertices}/S={S}")
+
+
+def test_csr_one_shot_entry_and_stats(native, oracle):
+    import ctypes as C
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.Auto)
+    try:
+        g = native.generate_graph500_rmat(10, 8, 8)
+        src = np.arange(0, 1024, 5, dtype=np.uint32)
+        out = np.empty(src.size * g.num_vertices, np.uint32)
+        st = native._native.Stats()
+        p = native._native.u32p
+        rc = native._native.lib().msbfs_run_ms_bfs_csr(
+            eng._h, g.num_vertices, g.num_edges, g.row_offsets.ctypes.data_as(p),
+            g.col_indices.ctypes.data_as(p), src.ctypes.data_as(p), src.size,
+            out.ctypes.data_as(p), C.byref(st))
+        assert rc == 0
+        want = _oracle(oracle, g, src)
+        assert_same(out, want, g, src, "csr one-shot")
+        assert st.reached_pairs == int(np.count_nonzero(want != 0xFFFFFFFF))
+        assert st.levels >= 2 and st.gpu_ms > 0
+    finally:
+        eng.close()
+
+
+def test_device_api_and_traversed_edges(native, gpu_engine, oracle):
+    torch = pytest.importorskip("torch")
+    g = native.generate_graph500_rmat(12, 16, 41)
+    src = native.sample_sources(g, 512, 3, min_degree=1)
+    out = torch.empty(src.size * g.num_vertices, dtype=torch.int32, device="cuda")
+    gpu_engine.run_ms_bfs_device(g, src, out.data_ptr())
+    st = gpu_engine.synchronize()
+    got = out.cpu().numpy().view(np.uint32)
+    want = _oracle(oracle, g, src)
+    assert_same(got, want, g, src, "device api")
+    assert st["path"] == 3 and st["pull_levels"] >= 1 and st["push_levels"] >= 1
+    te = gpu_engine.traversed_edges_device(g, out.data_ptr(), src.size)
+    assert te == oracle.traversed_edges(g.num_vertices, g.row_offsets, src.size, want)
+
+
+def test_host_loop_fallback(native, oracle, monkeypatch):
+    monkeypatch.setenv("MSBFS_HOST_LOOP", "1")
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.PushPullAdaptive)
+    try:
+        g = native.generate_graph500_rmat(11, 8, 13)
+        src = np.arange(0, 2048, 3, dtype=np.uint32)
+        got = eng.run_ms_bfs(g, src)
+        assert_same(got, _oracle(oracle, g, src), g, src, "host loop")
+    finally:
+        eng.close()

@@ -1,0 +1,146 @@
+"""ctypes binding of include/msbfs.h (libmsbfs.so).
+
+The shared library is built in-tree by webgpu_bfs_gb300/build.py. There is no
+fallback: if the library is missing or does not export the declared symbols,
+loading fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libmsbfs.so"
+
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+sizep = C.POINTER(C.c_size_t)
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("method", C.c_uint32),
+        ("path", C.c_uint32),
+        ("passes", C.c_uint32),
+        ("words_per_vertex", C.c_uint32),
+        ("levels", C.c_uint32),
+        ("push_levels", C.c_uint32),
+        ("pull_levels", C.c_uint32),
+        ("reserved0", C.c_uint32),
+        ("reached_pairs", C.c_uint64),
+        ("gpu_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved0"}
+
+
+class LevelRecord(C.Structure):
+    _fields_ = [
+        ("pass_", C.c_uint32),
+        ("level", C.c_uint32),
+        ("dir", C.c_uint32),
+        ("frontier_vertices", C.c_uint32),
+        ("frontier_entries", C.c_uint64),
+        ("active", C.c_uint64),
+        ("edges", C.c_uint64),
+        ("new_vertices", C.c_uint64),
+        ("new_pairs", C.c_uint64),
+        ("device_ms", C.c_double),
+        ("event_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["pass"] = d.pop("pass_")
+        return d
+
+
+class Csr(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_size_t),
+        ("num_edges", C.c_size_t),
+        ("row_offsets", u32p),
+        ("col_indices", u32p),
+    ]
+
+
+# name -> (restype, argtypes); every function declared in include/msbfs.h.
+SIGNATURES = {
+    "msbfs_engine_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "msbfs_engine_destroy": (None, [C.c_void_p]),
+    "msbfs_engine_method": (C.c_int, [C.c_void_p]),
+    "msbfs_engine_last_error": (C.c_char_p, [C.c_void_p]),
+    "msbfs_engine_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "msbfs_engine_set_tuning": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "msbfs_engine_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "msbfs_engine_level_log": (C.c_int, [C.c_void_p, C.POINTER(LevelRecord), C.c_size_t,
+                                         sizep]),
+    "msbfs_select_auto_method": (C.c_int, [C.c_size_t, C.c_size_t, u32p, C.c_size_t]),
+    "msbfs_graph_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, u32p, u32p,
+                                     C.POINTER(C.c_void_p)]),
+    "msbfs_graph_destroy": (None, [C.c_void_p]),
+    "msbfs_graph_info": (C.c_int, [C.c_void_p, sizep, sizep, u32p, C.POINTER(C.c_int)]),
+    "msbfs_run_ms_bfs": (C.c_int, [C.c_void_p, C.c_void_p, u32p, C.c_size_t, u32p,
+                                   C.POINTER(Stats)]),
+    "msbfs_run_ms_bfs_with_method": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, u32p,
+                                               C.c_size_t, u32p, C.POINTER(Stats)]),
+    "msbfs_run_ms_bfs_csr": (C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, u32p, u32p, u32p,
+                                       C.c_size_t, u32p, C.POINTER(Stats)]),
+    "msbfs_run_ms_bfs_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, u32p, C.c_size_t,
+                                          C.c_void_p]),
+    "msbfs_engine_synchronize": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "msbfs_run_reachability": (C.c_int, [C.c_void_p, C.c_void_p, u32p, C.c_size_t, u32p,
+                                         C.POINTER(Stats)]),
+    "msbfs_traversed_edges_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                               u64p]),
+    "msbfs_csr_free": (None, [C.POINTER(Csr)]),
+    "msbfs_csr_from_edge_list": (C.c_int, [C.c_size_t, C.c_size_t, u32p, u32p,
+                                           C.POINTER(Csr)]),
+    "msbfs_csr_transpose": (C.c_int, [C.POINTER(Csr), C.POINTER(Csr)]),
+    "msbfs_csr_is_symmetric": (C.c_int, [C.POINTER(Csr)]),
+    "msbfs_csr_to_undirected": (C.c_int, [C.POINTER(Csr), C.POINTER(Csr)]),
+    "msbfs_csr_validate": (C.c_int, [C.POINTER(Csr), C.c_char_p, C.c_size_t]),
+    "msbfs_csr_max_degree": (C.c_uint32, [C.POINTER(Csr)]),
+    "msbfs_gen_grid2d": (C.c_int, [C.c_size_t, C.c_size_t, C.POINTER(Csr)]),
+    "msbfs_gen_erdos_renyi_np": (C.c_int, [C.c_size_t, C.c_double, C.c_uint64,
+                                           C.POINTER(Csr)]),
+    "msbfs_gen_random_tree": (C.c_int, [C.c_size_t, C.c_uint64, C.POINTER(Csr)]),
+    "msbfs_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_uint64, C.c_int, C.POINTER(Csr)]),
+    "msbfs_gen_path": (C.c_int, [C.c_size_t, C.POINTER(Csr)]),
+    "msbfs_gen_star": (C.c_int, [C.c_size_t, C.POINTER(Csr)]),
+    "msbfs_gen_cycle": (C.c_int, [C.c_size_t, C.POINTER(Csr)]),
+    "msbfs_gen_clique": (C.c_int, [C.c_size_t, C.POINTER(Csr)]),
+    "msbfs_gen_disconnected_cliques": (C.c_int, [sizep, C.c_size_t, C.POINTER(Csr)]),
+    "msbfs_gen_wilson_grid": (C.c_int, [C.c_size_t, C.c_size_t, C.c_size_t, C.c_uint64,
+                                        C.POINTER(Csr)]),
+    "msbfs_sample_sources": (C.c_int, [C.POINTER(Csr), C.c_size_t, C.c_uint64, C.c_uint32,
+                                       u32p]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib() -> C.CDLL:
+    """Loads libmsbfs.so once and binds every declared entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = os.environ.get("MSBFS_LIB", str(LIB_PATH))
+        if not Path(path).exists():
+            raise ImportError(
+                f"libmsbfs.so not found at {path}; build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        handle = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)  # AttributeError if a symbol is missing
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib

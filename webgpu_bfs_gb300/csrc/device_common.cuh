@@ -1,0 +1,141 @@
+// Device-side data structures shared by the level-synchronous kernels, the
+// CTA-per-source kernel and the host orchestration (engine.cu).
+//
+// HBM layout of one level-synchronous pass over P <= 32*W sources:
+//   vis[V][W]        u32 visited bits, lane s of word s/32 = source s of the pass
+//   F[3][V][W]       frontier words, rotated by level: level L reads F[L%3],
+//                    writes F[(L+1)%3] and clears F[(L+2)%3] (= level L-1)
+//   planes[NP][V][W] bit-sliced discovery levels: bit b of d(s,v) is stored
+//                    in lane s of planes[b][v][s/32]; materialised into the
+//                    source-major u32 distance matrix once, after the loop
+//   ovf[V][W]        lanes whose distance did not fit NP planes; those were
+//                    written straight into the distance matrix
+//   Q[3][qcap]       u64 queue entries (seg << 32 | v): frontier vertices, one
+//                    entry per SEG out-edges so hub expansion is split
+//   stamp[V]         level at which v was last enqueued by a top-down step
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace msbfs {
+
+enum : uint32_t { DIR_PUSH = 0, DIR_PULL = 1 };
+enum : uint32_t { MODE_PUSH = 1, MODE_PULL = 2, MODE_HYBRID = 3 };
+enum : uint32_t { STATUS_LEVEL_CAP = 1u, STATUS_BAD_SOURCE = 2u };
+
+// Per-level record written by the level controller (counters feed the
+// algorithmic-bytes model of the roofline; t is %globaltimer ns).
+struct LevelRec {
+  uint32_t level;
+  uint32_t dir;
+  uint32_t frontier_vertices;  // |Q_L| vertices
+  uint32_t frontier_entries;   // |Q_L| entries (hub vertices split by seg)
+  unsigned long long active;   // bottom-up: vertex rows read (in-degree > 0)
+  unsigned long long edges;    // bottom-up: in-neighbour gathers; top-down: out-edges walked
+  unsigned long long new_vertices;
+  unsigned long long new_pairs;
+  unsigned long long t_start;
+  unsigned long long t_end;
+};
+
+constexpr uint32_t LOG_CAP = 4096;
+
+struct LevelCtl {
+  uint32_t level;      // frontier level L being expanded
+  uint32_t dir;        // direction of level L
+  uint32_t terminated; // 1 once a level discovered nothing
+  uint32_t status;     // STATUS_* bits
+  uint32_t qcount[4];  // queue entries per slot (slot 3 unused)
+  uint32_t qverts[4];  // vertices per slot
+  unsigned long long qedges[4];  // sum of out-degrees per slot
+  unsigned long long explored;   // out-edges of all expanded frontiers
+  unsigned long long pairs;      // discovered (s, v) pairs, sources included
+  uint32_t done_blocks;          // last-block-done counter of the level kernel
+  uint32_t push_levels;
+  uint32_t pull_levels;
+  uint32_t pad;
+  unsigned long long c_active;   // counters of the running level
+  unsigned long long c_edges;
+  unsigned long long c_newv;
+  unsigned long long c_pairs;
+  unsigned long long t_start;    // min %globaltimer over the level's blocks
+};
+
+// Per-pass descriptor, read from device memory so one captured CUDA graph can
+// serve every pass and every call.
+struct PassDesc {
+  const uint32_t* sources;  // this pass's sources (device)
+  uint32_t* dist;           // first row of this pass in the distance matrix
+  uint32_t* reach;          // non-null: write visited words here instead
+  uint32_t num_sources;     // P
+  uint32_t reach_wpv;       // words per vertex of the reachability output
+  uint32_t reach_col;       // word column of this pass in that output
+  uint32_t pad;
+};
+
+struct LevelParams {
+  uint32_t V;
+  uint32_t W;        // u32 words per vertex (template argument, repeated)
+  unsigned long long E;
+  const uint32_t* out_off;  // CSR: top-down steps
+  const uint32_t* out_idx;
+  const uint32_t* in_off;   // CSC: bottom-up steps (aliases CSR if symmetric)
+  const uint32_t* in_idx;
+  uint32_t* vis;
+  uint32_t* F[3];
+  uint32_t* planes;
+  uint32_t* ovf;
+  unsigned long long* Q[3];
+  uint32_t* stamp;
+  LevelCtl* ctl;
+  LevelRec* log;      // LOG_CAP records
+  const PassDesc* desc;
+  uint32_t NP;        // planes allocated
+  uint32_t qcap;
+  uint32_t mode;      // MODE_*
+  uint32_t alpha;     // push -> pull when m_f * alpha > unexplored edges
+  uint32_t beta;      // pull -> push when n_f * beta < V
+  uint32_t seg;       // out-edges per queue entry
+  uint32_t heavy;     // in-degree from which a whole warp scans one vertex
+  uint32_t max_levels;
+};
+
+// Launch helpers implemented in level_kernels.cu / cta_kernel.cu.
+struct LevelKernelInfo {
+  void* init;         // kernel symbols for graph nodes
+  void* level;
+  void* materialize;
+  void* cleanup;
+  int level_block;
+  int level_grid;
+  int mat_block;
+  int mat_grid;
+  size_t mat_smem;
+};
+// Fills kernel symbols and launch shapes for words-per-vertex W.
+bool level_kernel_info(uint32_t W, int num_sms, LevelKernelInfo* out);
+void launch_init(const LevelParams& p, cudaStream_t s);
+void launch_level(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s);
+void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s);
+void launch_cleanup(const LevelParams& p, cudaStream_t s);
+
+struct CtaParams {
+  uint32_t V;
+  const uint32_t* off;
+  const uint32_t* idx;
+  const uint32_t* sources;
+  uint32_t num_sources;
+  uint32_t* dist;        // row s at dist + s * V
+  uint32_t* gqueue;      // per resident block: 2 * V u32
+  uint32_t* work;        // source cursor (zeroed before launch)
+};
+// Max V for the shared-memory visited bitmap; grid/block for the CTA kernel.
+size_t cta_max_vertices(int device);
+bool cta_launch_shape(uint32_t V, int device, int* grid, int* block, size_t* smem);
+void launch_cta(const CtaParams& p, int grid, int block, size_t smem, cudaStream_t s);
+
+void launch_traversed_edges(uint32_t V, const uint32_t* off, const uint32_t* dist,
+                            uint32_t num_sources, unsigned long long* out, cudaStream_t s);
+
+}  // namespace msbfs

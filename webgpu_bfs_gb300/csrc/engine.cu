@@ -1,0 +1,935 @@
+// Engine: the C ABI of include/msbfs.h over the sm_103a kernels.
+//
+// Mirrors crates/gpu_bfs/src/engine.rs of the reference (GpuBfsEngine: method
+// enum, Auto router, per-call source validation, pooled device buffers behind
+// a mutex) with a CUDA runtime underneath instead of wgpu:
+//  * graphs are uploaded once and stay resident (CSR + CSC, aliased when the
+//    graph is symmetric, like PushPullGraphBuffers in buffer.rs:108-221);
+//  * a level-synchronous pass is ONE cudaGraphLaunch: memset control block,
+//    source init, a WHILE conditional node around the level kernel (its last
+//    block sets the condition, so no host round trip per level or per batch
+//    of levels, replacing multi_word_bp.rs:730-814's speculative 4..64-hop
+//    submits and indirect_sparse_push.rs:1462-1578's macro batches), the
+//    distance materialisation and the frontier cleanup;
+//  * the CTA-per-source path is one persistent launch per call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/msbfs.h"
+#include "device_common.cuh"
+#include "host_graph.h"
+
+using namespace msbfs;
+
+namespace {
+
+struct Workspace;
+
+}  // namespace
+
+struct msbfs_graph {
+  msbfs_engine* eng = nullptr;
+  uint64_t id = 0;
+  size_t V = 0, E = 0;
+  bool sym = false;
+  uint32_t max_deg = 0;
+  uint32_t* off = nullptr;   // CSR
+  uint32_t* idx = nullptr;
+  uint32_t* coff = nullptr;  // CSC (== CSR when symmetric)
+  uint32_t* cidx = nullptr;
+};
+
+namespace {
+
+struct Workspace {
+  uint64_t graph_id = 0;
+  uint32_t W = 0;
+  uint32_t mode = 0;
+  LevelParams p{};
+  LevelKernelInfo k{};
+  LevelCtl* d_ctl = nullptr;
+  PassDesc* d_desc = nullptr;
+  LevelRec* d_log = nullptr;
+  std::vector<void*> allocs;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~Workspace() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* a : allocs) cudaFree(a);
+  }
+};
+
+uint32_t bit_length_u64(uint64_t x) {
+  uint32_t n = 0;
+  while (x) {
+    ++n;
+    x >>= 1;
+  }
+  return n;
+}
+
+uint32_t method_path(int m) {
+  switch (m) {
+    case MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS:
+      return MSBFS_PATH_CTA;
+    case MSBFS_METHOD_MULTI_WORD_BIT_PARALLEL:
+    case MSBFS_METHOD_BIT_PARALLEL_64_PULL:
+    case MSBFS_METHOD_INDIRECT_MACRO_BATCH:
+      return MSBFS_PATH_PULL;
+    case MSBFS_METHOD_BIT_PARALLEL_32:
+    case MSBFS_METHOD_BIT_PARALLEL_64:
+    case MSBFS_METHOD_SPARSE_BIT_PARALLEL_64:
+    case MSBFS_METHOD_MULTI_WORD_BIT_PARALLEL_PUSH:
+    case MSBFS_METHOD_BOOLEAN_REACHABILITY:
+      return MSBFS_PATH_PUSH;
+    default:
+      return MSBFS_PATH_HYBRID;
+  }
+}
+
+}  // namespace
+
+struct msbfs_engine {
+  int device = 0;
+  int method = MSBFS_METHOD_AUTO;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_pass = nullptr, ev_copies = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  uint32_t max_words = 16;
+  uint32_t alpha = 14;
+  uint32_t beta = 24;
+  uint32_t seg = 64;
+  uint32_t heavy = 64;
+  bool host_loop = false;
+  int profiling = 0;
+  std::vector<msbfs_level_record> log;       // records of the last call
+  LevelRec* h_log = nullptr;                 // pinned, LOG_CAP per pass
+  size_t h_log_passes = 0;
+  std::vector<cudaEvent_t> lvl_events;       // profiling level 2
+  std::vector<std::vector<float>> pass_event_ms;
+  uint64_t next_graph_id = 1;
+  std::map<std::tuple<uint64_t, uint32_t, uint32_t>, std::unique_ptr<Workspace>> ws;
+  // call scratch
+  uint32_t* d_sources = nullptr;
+  size_t d_sources_cap = 0;
+  uint32_t* d_dist = nullptr;
+  size_t d_dist_cap = 0;  // u32 elements
+  uint32_t* d_reach = nullptr;
+  size_t d_reach_cap = 0;
+  uint32_t* d_cta_queue = nullptr;
+  size_t d_cta_queue_cap = 0;
+  uint32_t* d_work = nullptr;
+  unsigned long long* d_counter = nullptr;
+  LevelCtl* h_ctl = nullptr;  // pinned, one per pass of the last call
+  size_t h_ctl_cap = 0;
+  // last call
+  msbfs_stats last{};
+  size_t last_passes = 0;
+  bool last_level_path = false;
+};
+
+namespace {
+
+int set_err(msbfs_engine* e, int code, const std::string& msg) {
+  if (e) e->last_error = msg;
+  return code;
+}
+
+int cuda_fail(msbfs_engine* e, cudaError_t err, const char* what) {
+  cudaGetLastError();  // clear sticky-free errors
+  std::string m = std::string(what) + ": " + cudaGetErrorString(err);
+  return set_err(e, err == cudaErrorMemoryAllocation ? MSBFS_ERR_OOM : MSBFS_ERR_CUDA, m);
+}
+
+#define CK(call)                                            \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return cuda_fail(eng, _e, #call); \
+  } while (0)
+
+template <typename T>
+int grow(msbfs_engine* eng, T** ptr, size_t* cap, size_t need) {
+  if (need <= *cap && *ptr) return MSBFS_OK;
+  if (*ptr) {
+    // Earlier asynchronous calls may still read the old buffer.
+    CK(cudaStreamSynchronize(eng->stream));
+    CK(cudaStreamSynchronize(eng->copy_stream));
+    cudaFree(*ptr);
+  }
+  *ptr = nullptr;
+  *cap = 0;
+  size_t n = std::max(need, (size_t)1);
+  CK(cudaMalloc((void**)ptr, n * sizeof(T)));
+  *cap = n;
+  return MSBFS_OK;
+}
+
+int dev_alloc(msbfs_engine* eng, Workspace* w, void** ptr, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  CK(cudaMalloc(ptr, bytes));
+  w->allocs.push_back(*ptr);
+  CK(cudaMemsetAsync(*ptr, 0, bytes, eng->stream));
+  return MSBFS_OK;
+}
+
+int build_graph_exec(msbfs_engine* eng, Workspace* w) {
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  w->graph = g;
+  cudaGraphNode_t n_mctl, n_mst, n_init, n_cond, n_lvl, n_mat, n_clean;
+  cudaMemsetParams m1{};
+  m1.dst = w->d_ctl;
+  m1.value = 0;
+  m1.elementSize = 1;
+  m1.width = sizeof(LevelCtl);
+  m1.height = 1;
+  m1.pitch = sizeof(LevelCtl);
+  CK(cudaGraphAddMemsetNode(&n_mctl, g, nullptr, 0, &m1));
+  cudaMemsetParams m2{};
+  m2.dst = w->p.stamp;
+  m2.value = 0xFFFFFFFFu;
+  m2.elementSize = 4;
+  m2.width = w->p.V;
+  m2.height = 1;
+  m2.pitch = (size_t)w->p.V * 4;
+  CK(cudaGraphAddMemsetNode(&n_mst, g, nullptr, 0, &m2));
+
+  void* args_p[] = {&w->p};
+  cudaKernelNodeParams ki{};
+  ki.func = w->k.init;
+  ki.gridDim = dim3(1);
+  ki.blockDim = dim3(256);
+  ki.sharedMemBytes = 0;
+  ki.kernelParams = args_p;
+  cudaGraphNode_t deps_init[2] = {n_mctl, n_mst};
+  CK(cudaGraphAddKernelNode(&n_init, g, deps_init, 2, &ki));
+
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  CK(cudaGraphAddNode(&n_cond, g, &n_init, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+
+  void* args_l[] = {&w->p, &h};
+  cudaKernelNodeParams kl{};
+  kl.func = w->k.level;
+  kl.gridDim = dim3(w->k.level_grid);
+  kl.blockDim = dim3(w->k.level_block);
+  kl.sharedMemBytes = 0;
+  kl.kernelParams = args_l;
+  CK(cudaGraphAddKernelNode(&n_lvl, body, nullptr, 0, &kl));
+
+  cudaKernelNodeParams km{};
+  km.func = w->k.materialize;
+  km.gridDim = dim3(w->k.mat_grid);
+  km.blockDim = dim3(w->k.mat_block);
+  km.sharedMemBytes = (unsigned)w->k.mat_smem;
+  km.kernelParams = args_p;
+  CK(cudaGraphAddKernelNode(&n_mat, g, &n_cond, 1, &km));
+
+  cudaKernelNodeParams kc{};
+  kc.func = w->k.cleanup;
+  kc.gridDim = dim3(256);
+  kc.blockDim = dim3(256);
+  kc.sharedMemBytes = 0;
+  kc.kernelParams = args_p;
+  CK(cudaGraphAddKernelNode(&n_clean, g, &n_cond, 1, &kc));
+  (void)n_lvl;
+  (void)n_mat;
+  (void)n_clean;
+  CK(cudaGraphInstantiate(&w->exec, g, 0));
+  return MSBFS_OK;
+}
+
+int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t mode,
+                  Workspace** out) {
+  auto key = std::make_tuple(g->id, W, mode);
+  auto it = eng->ws.find(key);
+  if (it != eng->ws.end()) {
+    *out = it->second.get();
+    return MSBFS_OK;
+  }
+  // One pooled workspace per graph: drop any other (W, mode) of this graph
+  // only if memory runs short (allocation failure below retries once).
+  auto w = std::make_unique<Workspace>();
+  w->graph_id = g->id;
+  w->W = W;
+  w->mode = mode;
+  if (!level_kernel_info(W, eng->num_sms, &w->k))
+    return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "unsupported words per vertex");
+  LevelParams& p = w->p;
+  p.V = (uint32_t)g->V;
+  p.W = W;
+  p.E = g->E;
+  p.out_off = g->off;
+  p.out_idx = g->idx;
+  p.in_off = g->coff;
+  p.in_idx = g->cidx;
+  const size_t VW = g->V * (size_t)W;
+  const uint32_t dist_bits = bit_length_u64(g->V > 1 ? g->V - 1 : 1);
+  p.NP = std::min<uint32_t>(dist_bits, 8);
+  p.qcap = (uint32_t)std::min<uint64_t>(g->V + g->E / eng->seg + 1, 0xFFFFFFFFull);
+  p.mode = mode;
+  p.alpha = eng->alpha;
+  p.beta = eng->beta;
+  p.seg = eng->seg;
+  p.heavy = eng->heavy;
+  p.max_levels = (uint32_t)std::min<uint64_t>(g->V + 2, 0xFFFFFFF0ull);
+  int rc;
+  void* ptr;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4))) return rc;
+  p.vis = (uint32_t*)ptr;
+  for (int i = 0; i < 3; ++i) {
+    if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4))) return rc;
+    p.F[i] = (uint32_t*)ptr;
+  }
+  if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4 * (size_t)p.NP))) return rc;
+  p.planes = (uint32_t*)ptr;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4))) return rc;
+  p.ovf = (uint32_t*)ptr;
+  for (int i = 0; i < 3; ++i) {
+    if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)p.qcap * 8))) return rc;
+    p.Q[i] = (unsigned long long*)ptr;
+  }
+  if ((rc = dev_alloc(eng, w.get(), &ptr, g->V * 4))) return rc;
+  p.stamp = (uint32_t*)ptr;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, sizeof(LevelCtl)))) return rc;
+  w->d_ctl = (LevelCtl*)ptr;
+  p.ctl = w->d_ctl;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, sizeof(PassDesc)))) return rc;
+  w->d_desc = (PassDesc*)ptr;
+  p.desc = w->d_desc;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, sizeof(LevelRec) * LOG_CAP))) return rc;
+  w->d_log = (LevelRec*)ptr;
+  p.log = w->d_log;
+  if (!eng->host_loop) {
+    rc = build_graph_exec(eng, w.get());
+    if (rc) {
+      // Conditional graph nodes unavailable: fall back to the host-driven loop.
+      eng->host_loop = true;
+      cudaGetLastError();
+    }
+  }
+  *out = w.get();
+  eng->ws[key] = std::move(w);
+  return MSBFS_OK;
+}
+
+// Host-driven fallback loop: launches level kernels in speculative batches of
+// 8 and reads the control block between batches (extra launches after the
+// last level return immediately).
+int ensure_events(msbfs_engine* eng, size_t n) {
+  while (eng->lvl_events.size() < n) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    eng->lvl_events.push_back(e);
+  }
+  return MSBFS_OK;
+}
+
+// Profiling form of the host-driven loop: one level kernel at a time with a
+// CUDA event on each side, then the materialisation likewise. The last entry
+// of the returned vector is the materialisation.
+int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
+  int rc;
+  CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
+  CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
+  launch_init(w->p, eng->stream);
+  LevelCtl probe{};
+  ms->clear();
+  for (uint32_t L = 0;; ++L) {
+    if ((rc = ensure_events(eng, 2))) return rc;
+    CK(cudaEventRecord(eng->lvl_events[0], eng->stream));
+    launch_level(w->p, w->k, eng->stream);
+    CK(cudaEventRecord(eng->lvl_events[1], eng->stream));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&probe, w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost, eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, eng->lvl_events[0], eng->lvl_events[1]);
+    ms->push_back(t);
+    if (probe.terminated) break;
+    if (L > w->p.max_levels) return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
+  }
+  CK(cudaEventRecord(eng->lvl_events[0], eng->stream));
+  launch_materialize(w->p, w->k, eng->stream);
+  CK(cudaEventRecord(eng->lvl_events[1], eng->stream));
+  launch_cleanup(w->p, eng->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(eng->stream));
+  float t = 0.f;
+  cudaEventElapsedTime(&t, eng->lvl_events[0], eng->lvl_events[1]);
+  ms->push_back(t);
+  return MSBFS_OK;
+}
+
+int run_pass_host_loop(msbfs_engine* eng, Workspace* w) {
+  CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
+  CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
+  launch_init(w->p, eng->stream);
+  LevelCtl probe{};
+  for (uint64_t launched = 0;;) {
+    for (int i = 0; i < 8; ++i) launch_level(w->p, w->k, eng->stream);
+    launched += 8;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&probe, w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost, eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    if (probe.terminated) break;
+    if (launched > (uint64_t)w->p.max_levels + 16)
+      return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
+  }
+  launch_materialize(w->p, w->k, eng->stream);
+  launch_cleanup(w->p, eng->stream);
+  CK(cudaGetLastError());
+  return MSBFS_OK;
+}
+
+uint32_t choose_words(msbfs_engine* eng, size_t S) {
+  size_t lanes = std::min<size_t>(S, (size_t)eng->max_words * 32);
+  uint32_t need = (uint32_t)((lanes + 31) / 32);
+  uint32_t W = 1;
+  while (W < need) W <<= 1;
+  return std::min<uint32_t>(W, 64);
+}
+
+int validate_call(msbfs_engine* eng, const msbfs_graph* g, const uint32_t* sources, size_t S) {
+  if (!eng) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (!g) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "graph is null");
+  if (g->eng != eng) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "graph belongs to another engine");
+  if (S == 0) return MSBFS_OK;
+  if (!sources) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "sources is null");
+  char buf[160];
+  if (g->V == 0) {
+    snprintf(buf, sizeof buf, "Source vertex %u at index 0 exceeds graph vertex count 0", sources[0]);
+    return set_err(eng, MSBFS_ERR_EMPTY_GRAPH, buf);
+  }
+  for (size_t i = 0; i < S; ++i)
+    if ((size_t)sources[i] >= g->V) {
+      snprintf(buf, sizeof buf, "Source vertex %u at index %zu exceeds graph vertex count %zu",
+               sources[i], i, g->V);
+      return set_err(eng, MSBFS_ERR_SOURCE_OOB, buf);
+    }
+  return MSBFS_OK;
+}
+
+int resolve_method(const msbfs_graph* g, int method, size_t S) {
+  if (method == MSBFS_METHOD_AUTO) {
+    if (g->V == 0 || S == 0) return MSBFS_METHOD_NAIVE_SEQUENTIAL;
+    const bool road = g->max_deg <= 8 && g->E <= 4 * g->V;
+    if (road) return MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS;
+    if (g->max_deg >= 128) return MSBFS_METHOD_INDIRECT_SPARSE_QUEUE_PUSH;
+    if (S >= 64) return MSBFS_METHOD_MULTI_WORD_BIT_PARALLEL;
+    if (S >= 32) return MSBFS_METHOD_BIT_PARALLEL_64;
+    if (S > 1) return MSBFS_METHOD_BIT_PARALLEL_32;
+    return MSBFS_METHOD_SPARSE_QUEUE;
+  }
+  return method;
+}
+
+// Queues a whole call on eng->stream. dist_dev: S*V output (device) or null
+// in reachability mode; reach_dev: V*ceil(S/32) words (device) or null.
+// host_out / host_reach: when non-null, rows are copied back per pass on the
+// copy stream while later passes run.
+int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t* sources,
+                 size_t S, uint32_t* dist_dev, uint32_t* reach_dev, uint32_t* host_out,
+                 uint32_t* host_reach) {
+  int rc;
+  const int m = resolve_method(g, method, S);
+  uint32_t path = method_path(m);
+  if (reach_dev && path == MSBFS_PATH_CTA) path = MSBFS_PATH_HYBRID;
+  int cta_grid = 0, cta_block = 0;
+  size_t cta_smem = 0;
+  if (path == MSBFS_PATH_CTA &&
+      !cta_launch_shape((uint32_t)g->V, eng->device, &cta_grid, &cta_block, &cta_smem))
+    path = MSBFS_PATH_HYBRID;
+  if (!g->sym && path != MSBFS_PATH_CTA && !g->coff)
+    return set_err(eng, MSBFS_ERR_INVALID_GRAPH, "missing transpose");
+
+  eng->last = msbfs_stats{};
+  eng->last.method = (uint32_t)m;
+  eng->last.path = path;
+  eng->last_level_path = path != MSBFS_PATH_CTA;
+  if ((rc = grow(eng, &eng->d_sources, &eng->d_sources_cap, S))) return rc;
+  CK(cudaEventRecord(eng->ev_start, eng->stream));
+  CK(cudaMemcpyAsync(eng->d_sources, sources, S * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                     eng->stream));
+  const size_t V = g->V;
+
+  if (path == MSBFS_PATH_CTA) {
+    const size_t slabs = (size_t)cta_grid * 2 * V;
+    if ((rc = grow(eng, &eng->d_cta_queue, &eng->d_cta_queue_cap, slabs))) return rc;
+    CK(cudaMemsetAsync(eng->d_work, 0, sizeof(uint32_t), eng->stream));
+    CtaParams cp{};
+    cp.V = (uint32_t)V;
+    cp.off = g->off;
+    cp.idx = g->idx;
+    cp.sources = eng->d_sources;
+    cp.num_sources = (uint32_t)S;
+    cp.dist = dist_dev;
+    cp.gqueue = eng->d_cta_queue;
+    cp.work = eng->d_work;
+    launch_cta(cp, std::min<int>(cta_grid, (int)S), cta_block, cta_smem, eng->stream);
+    CK(cudaGetLastError());
+    eng->last.passes = 1;
+    eng->last_passes = 0;
+    if (host_out) {
+      CK(cudaMemcpyAsync(host_out, dist_dev, S * V * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                         eng->stream));
+    }
+    CK(cudaEventRecord(eng->ev_stop, eng->stream));
+    return MSBFS_OK;
+  }
+
+  const uint32_t mode = path == MSBFS_PATH_PUSH   ? MODE_PUSH
+                        : path == MSBFS_PATH_PULL ? MODE_PULL
+                                                  : MODE_HYBRID;
+  const uint32_t W = choose_words(eng, S);
+  const size_t PW = (size_t)W * 32;
+  const size_t passes = (S + PW - 1) / PW;
+  Workspace* w = nullptr;
+  if ((rc = get_workspace(eng, g, W, mode, &w))) return rc;
+  if (passes > eng->h_ctl_cap) {
+    CK(cudaStreamSynchronize(eng->stream));
+    if (eng->h_ctl) cudaFreeHost(eng->h_ctl);
+    eng->h_ctl = nullptr;
+    eng->h_ctl_cap = 0;
+    CK(cudaMallocHost((void**)&eng->h_ctl, passes * sizeof(LevelCtl)));
+    eng->h_ctl_cap = passes;
+  }
+  eng->last.passes = (uint32_t)passes;
+  eng->last.words_per_vertex = W;
+  eng->last_passes = passes;
+  if (eng->profiling) {
+    if (passes > eng->h_log_passes) {
+      CK(cudaStreamSynchronize(eng->stream));
+      if (eng->h_log) cudaFreeHost(eng->h_log);
+      eng->h_log = nullptr;
+      eng->h_log_passes = 0;
+      CK(cudaMallocHost((void**)&eng->h_log, passes * LOG_CAP * sizeof(LevelRec)));
+      eng->h_log_passes = passes;
+    }
+    eng->pass_event_ms.assign(passes, {});
+  }
+  const size_t wpv = (S + 31) / 32;
+  for (size_t ps = 0; ps < passes; ++ps) {
+    const size_t s0 = ps * PW;
+    const size_t np = std::min(PW, S - s0);
+    PassDesc d{};
+    d.sources = eng->d_sources + s0;
+    d.dist = dist_dev ? dist_dev + s0 * V : nullptr;
+    d.reach = reach_dev;
+    d.num_sources = (uint32_t)np;
+    d.reach_wpv = (uint32_t)wpv;
+    d.reach_col = (uint32_t)(ps * W);
+    // Pageable source: the copy is staged before the call returns, so the
+    // stack descriptor can go out of scope.
+    CK(cudaMemcpyAsync(w->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, eng->stream));
+    if (eng->profiling >= 2) {
+      if ((rc = run_pass_profiled(eng, w, &eng->pass_event_ms[ps]))) return rc;
+    } else if (w->exec && !eng->host_loop) {
+      CK(cudaGraphLaunch(w->exec, eng->stream));
+    } else {
+      if ((rc = run_pass_host_loop(eng, w))) return rc;
+    }
+    CK(cudaMemcpyAsync(&eng->h_ctl[ps], w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost,
+                       eng->stream));
+    if (eng->profiling)
+      CK(cudaMemcpyAsync(eng->h_log + ps * LOG_CAP, w->d_log, LOG_CAP * sizeof(LevelRec),
+                         cudaMemcpyDeviceToHost, eng->stream));
+    if (host_out) {
+      CK(cudaEventRecord(eng->ev_pass, eng->stream));
+      CK(cudaStreamWaitEvent(eng->copy_stream, eng->ev_pass, 0));
+      CK(cudaMemcpyAsync(host_out + s0 * V, dist_dev + s0 * V, np * V * sizeof(uint32_t),
+                         cudaMemcpyDeviceToHost, eng->copy_stream));
+    }
+  }
+  if (host_reach) {
+    CK(cudaMemcpyAsync(host_reach, reach_dev, V * wpv * sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost, eng->stream));
+  }
+  if (host_out) {
+    CK(cudaEventRecord(eng->ev_copies, eng->copy_stream));
+    CK(cudaStreamWaitEvent(eng->stream, eng->ev_copies, 0));
+  }
+  CK(cudaEventRecord(eng->ev_stop, eng->stream));
+  return MSBFS_OK;
+}
+
+int finish_call(msbfs_engine* eng, msbfs_stats* stats) {
+  CK(cudaEventSynchronize(eng->ev_stop));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, eng->ev_start, eng->ev_stop);
+  eng->last.gpu_ms = ms;
+  uint32_t status = 0;
+  for (size_t i = 0; i < eng->last_passes; ++i) {
+    const LevelCtl& c = eng->h_ctl[i];
+    eng->last.levels = std::max(eng->last.levels, c.level + 1);
+    eng->last.push_levels += c.push_levels;
+    eng->last.pull_levels += c.pull_levels;
+    eng->last.reached_pairs += c.pairs;
+    status |= c.status;
+  }
+  eng->log.clear();
+  if (eng->profiling && eng->h_log) {
+    for (size_t ps = 0; ps < eng->last_passes; ++ps) {
+      const LevelCtl& c = eng->h_ctl[ps];
+      const uint32_t nlev = std::min<uint32_t>(c.level + 1, LOG_CAP);
+      const std::vector<float>* ev =
+          ps < eng->pass_event_ms.size() ? &eng->pass_event_ms[ps] : nullptr;
+      for (uint32_t L = 0; L < nlev; ++L) {
+        const LevelRec& r = eng->h_log[ps * LOG_CAP + L];
+        msbfs_level_record o{};
+        o.pass = (uint32_t)ps;
+        o.level = r.level;
+        o.dir = r.dir;
+        o.frontier_vertices = r.frontier_vertices;
+        o.frontier_entries = r.frontier_entries;
+        o.active = r.active;
+        o.edges = r.edges;
+        o.new_vertices = r.new_vertices;
+        o.new_pairs = r.new_pairs;
+        o.device_ms = r.t_end > r.t_start ? (double)(r.t_end - r.t_start) * 1e-6 : 0.0;
+        o.event_ms = (ev && L < ev->size() && !ev->empty()) ? (*ev)[L] : 0.0;
+        eng->log.push_back(o);
+      }
+      if (ev && !ev->empty()) {
+        msbfs_level_record m{};
+        m.pass = (uint32_t)ps;
+        m.level = c.level;
+        m.dir = MSBFS_DIR_MATERIALIZE;
+        m.event_ms = ev->back();
+        eng->log.push_back(m);
+      }
+    }
+  }
+  if (stats) *stats = eng->last;
+  if (status & STATUS_LEVEL_CAP) return set_err(eng, MSBFS_ERR_TIMEOUT, "level cap reached");
+  if (status & STATUS_BAD_SOURCE) return set_err(eng, MSBFS_ERR_SOURCE_OOB, "source out of range");
+  return MSBFS_OK;
+}
+
+int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, const uint32_t* idx,
+                 msbfs_graph** out) {
+  if (!eng || !out) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (V >= 0xFFFFFFFFull || E > 0xFFFFFFFFull)
+    return set_err(eng, MSBFS_ERR_INVALID_GRAPH, "graph exceeds u32 indices");
+  std::string why = msbfs::validate(V, E, off, idx, E);
+  if (!why.empty()) return set_err(eng, MSBFS_ERR_INVALID_GRAPH, why);
+  auto g = std::make_unique<msbfs_graph>();
+  g->eng = eng;
+  g->id = eng->next_graph_id++;
+  g->V = V;
+  g->E = E;
+  g->max_deg = msbfs::max_degree(V, off);
+  msbfs::HostCsr t = msbfs::transpose(V, E, off, idx);
+  g->sym = std::equal(t.off.begin(), t.off.end(), off) &&
+           (E == 0 || std::memcmp(t.idx.data(), idx, E * 4) == 0);
+  CK(cudaSetDevice(eng->device));
+  CK(cudaMalloc((void**)&g->off, (V + 1) * 4));
+  CK(cudaMalloc((void**)&g->idx, std::max<size_t>(E, 1) * 4));
+  CK(cudaMemcpy(g->off, off, (V + 1) * 4, cudaMemcpyHostToDevice));
+  if (E) CK(cudaMemcpy(g->idx, idx, E * 4, cudaMemcpyHostToDevice));
+  if (g->sym) {
+    g->coff = g->off;
+    g->cidx = g->idx;
+  } else {
+    CK(cudaMalloc((void**)&g->coff, (V + 1) * 4));
+    CK(cudaMalloc((void**)&g->cidx, std::max<size_t>(E, 1) * 4));
+    CK(cudaMemcpy(g->coff, t.off.data(), (V + 1) * 4, cudaMemcpyHostToDevice));
+    if (E) CK(cudaMemcpy(g->cidx, t.idx.data(), E * 4, cudaMemcpyHostToDevice));
+  }
+  *out = g.release();
+  return MSBFS_OK;
+}
+
+void free_graph(msbfs_graph* g) {
+  if (!g) return;
+  msbfs_engine* eng = g->eng;
+  if (eng) {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    cudaSetDevice(eng->device);
+    cudaStreamSynchronize(eng->stream);
+    for (auto it = eng->ws.begin(); it != eng->ws.end();)
+      if (std::get<0>(it->first) == g->id)
+        it = eng->ws.erase(it);
+      else
+        ++it;
+  }
+  if (!g->sym) {
+    cudaFree(g->coff);
+    cudaFree(g->cidx);
+  }
+  cudaFree(g->off);
+  cudaFree(g->idx);
+  delete g;
+}
+
+// Blocking run into caller-owned host memory.
+int run_host(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t* sources,
+             size_t S, uint32_t* out, msbfs_stats* stats) {
+  int rc = validate_call(eng, g, sources, S);
+  if (rc) return rc;
+  if (stats) *stats = msbfs_stats{};
+  if (S == 0) return MSBFS_OK;
+  if (!out) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "out is null");
+  CK(cudaSetDevice(eng->device));
+  const size_t total = S * g->V;
+  if ((rc = grow(eng, &eng->d_dist, &eng->d_dist_cap, total))) return rc;
+  if ((rc = enqueue_call(eng, method, g, sources, S, eng->d_dist, nullptr, out, nullptr)))
+    return rc;
+  return finish_call(eng, stats);
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+int msbfs_engine_create(int device, int method, msbfs_engine** out) {
+  if (!out) return MSBFS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (method < 0 || method > MSBFS_METHOD_AUTO) return MSBFS_ERR_INVALID_ARGUMENT;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return MSBFS_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return MSBFS_ERR_NO_DEVICE;
+  auto eng = std::make_unique<msbfs_engine>();
+  eng->device = device;
+  eng->method = method;
+  msbfs_engine* e = eng.get();
+  if (cudaSetDevice(device) != cudaSuccess) return MSBFS_ERR_CUDA;
+  cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e->ev_start) != cudaSuccess || cudaEventCreate(&e->ev_stop) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_pass, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_copies, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMalloc((void**)&e->d_work, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc((void**)&e->d_counter, sizeof(unsigned long long)) != cudaSuccess)
+    return MSBFS_ERR_CUDA;
+  e->stream = e->own_stream;
+  const char* hl = getenv("MSBFS_HOST_LOOP");
+  e->host_loop = hl && hl[0] == '1';
+  *out = eng.release();
+  return MSBFS_OK;
+}
+
+void msbfs_engine_destroy(msbfs_engine* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->stream);
+  cudaStreamSynchronize(e->copy_stream);
+  e->ws.clear();
+  cudaFree(e->d_sources);
+  cudaFree(e->d_dist);
+  cudaFree(e->d_reach);
+  cudaFree(e->d_cta_queue);
+  cudaFree(e->d_work);
+  cudaFree(e->d_counter);
+  if (e->h_ctl) cudaFreeHost(e->h_ctl);
+  if (e->h_log) cudaFreeHost(e->h_log);
+  for (cudaEvent_t ev : e->lvl_events) cudaEventDestroy(ev);
+  cudaEventDestroy(e->ev_start);
+  cudaEventDestroy(e->ev_stop);
+  cudaEventDestroy(e->ev_pass);
+  cudaEventDestroy(e->ev_copies);
+  cudaStreamDestroy(e->own_stream);
+  cudaStreamDestroy(e->copy_stream);
+  delete e;
+}
+
+int msbfs_engine_method(const msbfs_engine* e) { return e ? e->method : -1; }
+
+const char* msbfs_engine_last_error(const msbfs_engine* e) {
+  return e ? e->last_error.c_str() : "null engine";
+}
+
+int msbfs_engine_set_stream(msbfs_engine* e, void* s) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->stream = s ? (cudaStream_t)s : e->own_stream;
+  return MSBFS_OK;
+}
+
+int msbfs_engine_set_tuning(msbfs_engine* e, uint32_t max_words, uint32_t alpha, uint32_t beta) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  if (max_words) {
+    if (max_words > 64 || (max_words & (max_words - 1)))
+      return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "max_words_per_pass must be a power of two <= 64");
+    e->max_words = max_words;
+  }
+  if (alpha) e->alpha = alpha;
+  if (beta) e->beta = beta;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->stream);
+  e->ws.clear();  // thresholds are baked into the captured graphs
+  return MSBFS_OK;
+}
+
+int msbfs_engine_set_profiling(msbfs_engine* e, int level) {
+  if (!e || level < 0 || level > 2) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->profiling = level;
+  return MSBFS_OK;
+}
+
+int msbfs_engine_level_log(const msbfs_engine* e, msbfs_level_record* out, size_t cap,
+                           size_t* count) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  const size_t n = e->log.size();
+  if (count) *count = n;
+  if (out) std::memcpy(out, e->log.data(), std::min(cap, n) * sizeof(msbfs_level_record));
+  return MSBFS_OK;
+}
+
+int msbfs_select_auto_method(size_t V, size_t E, const uint32_t* off, size_t S) {
+  msbfs_graph g;
+  g.V = V;
+  g.E = E;
+  g.max_deg = (V && off) ? msbfs::max_degree(V, off) : 0;
+  return resolve_method(&g, MSBFS_METHOD_AUTO, S);
+}
+
+int msbfs_graph_create(msbfs_engine* e, size_t V, size_t E, const uint32_t* off,
+                       const uint32_t* idx, msbfs_graph** out) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  return upload_graph(e, V, E, off, idx, out);
+}
+
+void msbfs_graph_destroy(msbfs_graph* g) { free_graph(g); }
+
+int msbfs_graph_info(const msbfs_graph* g, size_t* V, size_t* E, uint32_t* max_deg, int* sym) {
+  if (!g) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (V) *V = g->V;
+  if (E) *E = g->E;
+  if (max_deg) *max_deg = g->max_deg;
+  if (sym) *sym = g->sym ? 1 : 0;
+  return MSBFS_OK;
+}
+
+int msbfs_run_ms_bfs(msbfs_engine* e, const msbfs_graph* g, const uint32_t* sources, size_t S,
+                     uint32_t* out, msbfs_stats* stats) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  return run_host(e, e->method, g, sources, S, out, stats);
+}
+
+int msbfs_run_ms_bfs_with_method(msbfs_engine* e, int method, const msbfs_graph* g,
+                                 const uint32_t* sources, size_t S, uint32_t* out,
+                                 msbfs_stats* stats) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (method < 0 || method > MSBFS_METHOD_AUTO)
+    return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "unknown method");
+  std::lock_guard<std::mutex> lk(e->mu);
+  return run_host(e, method, g, sources, S, out, stats);
+}
+
+int msbfs_run_ms_bfs_csr(msbfs_engine* e, size_t V, size_t E, const uint32_t* off,
+                         const uint32_t* idx, const uint32_t* sources, size_t S, uint32_t* out,
+                         msbfs_stats* stats) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (S == 0) {
+    if (stats) *stats = msbfs_stats{};
+    return MSBFS_OK;
+  }
+  msbfs_graph* g = nullptr;
+  int rc;
+  {
+    std::lock_guard<std::mutex> lk(e->mu);
+    rc = upload_graph(e, V, E, off, idx, &g);
+    if (rc == MSBFS_OK) rc = run_host(e, e->method, g, sources, S, out, stats);
+  }
+  free_graph(g);
+  return rc;
+}
+
+int msbfs_run_ms_bfs_device(msbfs_engine* e, int method, const msbfs_graph* g,
+                            const uint32_t* sources, size_t S, uint32_t* out_device) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (method < 0 || method > MSBFS_METHOD_AUTO)
+    return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "unknown method");
+  std::lock_guard<std::mutex> lk(e->mu);
+  msbfs_engine* eng = e;
+  int rc = validate_call(e, g, sources, S);
+  if (rc) return rc;
+  e->last = msbfs_stats{};
+  e->last_passes = 0;
+  if (S == 0) {
+    CK(cudaEventRecord(e->ev_start, e->stream));
+    CK(cudaEventRecord(e->ev_stop, e->stream));
+    return MSBFS_OK;
+  }
+  if (!out_device) return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "out is null");
+  CK(cudaSetDevice(e->device));
+  return enqueue_call(e, method, g, sources, S, out_device, nullptr, nullptr, nullptr);
+}
+
+int msbfs_engine_synchronize(msbfs_engine* e, msbfs_stats* stats) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  return finish_call(e, stats);
+}
+
+int msbfs_run_reachability(msbfs_engine* e, const msbfs_graph* g, const uint32_t* sources,
+                           size_t S, uint32_t* words, msbfs_stats* stats) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  msbfs_engine* eng = e;
+  int rc = validate_call(e, g, sources, S);
+  if (rc) return rc;
+  if (stats) *stats = msbfs_stats{};
+  if (S == 0 || g->V == 0) return MSBFS_OK;
+  if (!words) return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "words is null");
+  CK(cudaSetDevice(e->device));
+  const size_t wpv = (S + 31) / 32;
+  if ((rc = grow(e, &e->d_reach, &e->d_reach_cap, g->V * wpv))) return rc;
+  int method = e->method;
+  if (resolve_method(g, method, S) == MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS)
+    method = MSBFS_METHOD_PUSH_PULL_ADAPTIVE;
+  if ((rc = enqueue_call(e, method, g, sources, S, nullptr, e->d_reach, nullptr, words)))
+    return rc;
+  return finish_call(e, stats);
+}
+
+int msbfs_traversed_edges_device(msbfs_engine* e, const msbfs_graph* g, const uint32_t* dist,
+                                 size_t S, uint64_t* out_edges) {
+  if (!e || !g || !out_edges) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  msbfs_engine* eng = e;
+  *out_edges = 0;
+  if (S == 0 || g->V == 0) return MSBFS_OK;
+  CK(cudaSetDevice(e->device));
+  launch_traversed_edges((uint32_t)g->V, g->off, dist, (uint32_t)S, e->d_counter, e->stream);
+  CK(cudaGetLastError());
+  unsigned long long h = 0;
+  CK(cudaMemcpyAsync(&h, e->d_counter, sizeof h, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  *out_edges = h;
+  return MSBFS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,859 @@
+// Level-synchronous bit-parallel multi-source BFS kernels for sm_103a.
+//
+// One pass traverses up to 32*W sources at once: lane s of word s/32 of a
+// vertex's W-word row belongs to source s. A level is one launch of
+// level_kernel<W>, which runs either a bottom-up (pull) or a top-down (push)
+// step, as decided on the device by the previous level; the loop itself is a
+// CUDA-graph WHILE node whose condition the last block of each level sets.
+//
+// Semantics follow the reference's WGSL kernels:
+//   bottom-up step  crates/shaders/src/multi_word_bp_pull_512.wgsl:69-138
+//                   (needed = ~vis & mask; cand = OR of in-neighbours' frontier
+//                   words with early exit once cand covers needed;
+//                   newly = cand & needed)
+//   top-down step   crates/shaders/src/indirect_sparse_push_512.wgsl:89-321
+//                   (needed = f & ~vis; prev = atomicOr(vis, needed);
+//                   newly = needed & ~prev; one enqueue per vertex per level)
+//   direction       crates/shaders/src/prep_hybrid_hop.wgsl:46-134 and the
+//                   host alpha/beta rule of crates/gpu_bfs/src/dispatch/
+//                   push_pull.rs:484-498
+//   source init     crates/shaders/src/init_sparse_push_sources_512.wgsl:27-67
+// The GB300 design (vectorised 16-byte frontier gathers per lane group, a
+// warp per heavy vertex, warp-aggregated atomics, block-staged queue
+// compaction, bit-sliced level planes materialised into coalesced rows) is
+// this file's own.
+#include <cooperative_groups.h>
+
+#include "device_common.cuh"
+
+namespace msbfs {
+
+constexpr int LEVEL_BLOCK = 256;
+constexpr int BQ_CAP = 2048;  // discovered vertices staged per block
+constexpr int CH = 4;         // in-neighbours gathered per chunk
+constexpr int MAT_KC = 8;     // words per materialise chunk
+constexpr int MAT_BLOCK = 256;
+constexpr uint32_t FULL = 0xffffffffu;
+constexpr uint32_t DIST_MAX = 0xffffffffu;
+
+template <int W>
+struct Geo {
+  static constexpr int VEC = W >= 4 ? 4 : W;  // words per lane access
+  static constexpr int LPV = W / VEC;         // lanes per vertex (a "group")
+  static constexpr int GPW = 32 / LPV;        // groups per warp
+};
+
+template <int VEC>
+struct Words {
+  uint32_t w[VEC];
+};
+
+template <int VEC>
+__device__ __forceinline__ Words<VEC> ld_words(const uint32_t* p) {
+  Words<VEC> r;
+  if constexpr (VEC == 4) {
+    uint4 t = *reinterpret_cast<const uint4*>(p);
+    r.w[0] = t.x; r.w[1] = t.y; r.w[2] = t.z; r.w[3] = t.w;
+  } else if constexpr (VEC == 2) {
+    uint2 t = *reinterpret_cast<const uint2*>(p);
+    r.w[0] = t.x; r.w[1] = t.y;
+  } else {
+    r.w[0] = *p;
+  }
+  return r;
+}
+
+// Read-only path: frontier words of the level being expanded and the graph.
+template <int VEC>
+__device__ __forceinline__ Words<VEC> ldg_words(const uint32_t* p) {
+  Words<VEC> r;
+  if constexpr (VEC == 4) {
+    uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
+    r.w[0] = t.x; r.w[1] = t.y; r.w[2] = t.z; r.w[3] = t.w;
+  } else if constexpr (VEC == 2) {
+    uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+    r.w[0] = t.x; r.w[1] = t.y;
+  } else {
+    r.w[0] = __ldg(p);
+  }
+  return r;
+}
+
+// L2-coherent read of words other blocks update with atomics this level.
+template <int VEC>
+__device__ __forceinline__ Words<VEC> ldcg_words(const uint32_t* p) {
+  Words<VEC> r;
+  if constexpr (VEC == 4) {
+    uint4 t = __ldcg(reinterpret_cast<const uint4*>(p));
+    r.w[0] = t.x; r.w[1] = t.y; r.w[2] = t.z; r.w[3] = t.w;
+  } else if constexpr (VEC == 2) {
+    uint2 t = __ldcg(reinterpret_cast<const uint2*>(p));
+    r.w[0] = t.x; r.w[1] = t.y;
+  } else {
+    r.w[0] = __ldcg(p);
+  }
+  return r;
+}
+
+template <int VEC>
+__device__ __forceinline__ void st_words(uint32_t* p, const Words<VEC>& r) {
+  if constexpr (VEC == 4) {
+    *reinterpret_cast<uint4*>(p) = make_uint4(r.w[0], r.w[1], r.w[2], r.w[3]);
+  } else if constexpr (VEC == 2) {
+    *reinterpret_cast<uint2*>(p) = make_uint2(r.w[0], r.w[1]);
+  } else {
+    *p = r.w[0];
+  }
+}
+
+template <int VEC>
+__device__ __forceinline__ bool any_bits(const Words<VEC>& a) {
+  uint32_t x = 0;
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) x |= a.w[j];
+  return x != 0;
+}
+
+__device__ __forceinline__ uint32_t nseg_of(uint32_t deg, uint32_t seg) {
+  return deg ? (deg + seg - 1) / seg : 1u;
+}
+
+struct BlockQueue {
+  uint32_t items[BQ_CAP];
+  uint32_t count;
+  uint32_t base;
+  uint32_t warp_sum[LEVEL_BLOCK / 32];
+  unsigned long long warp_edges[LEVEL_BLOCK / 32];
+};
+
+// Enqueue straight into the global queue (sources, and blocks whose staging
+// area is full). Entry i of vertex v covers out-edges [i*seg, (i+1)*seg).
+__device__ void enqueue_global(const LevelParams& p, uint32_t slot, uint32_t v) {
+  const uint32_t deg = p.out_off[v + 1] - p.out_off[v];
+  const uint32_t n = nseg_of(deg, p.seg);
+  const uint32_t base = atomicAdd(&p.ctl->qcount[slot], n);
+  atomicAdd(&p.ctl->qverts[slot], 1u);
+  atomicAdd(&p.ctl->qedges[slot], (unsigned long long)deg);
+  for (uint32_t i = 0; i < n; ++i)
+    p.Q[slot][base + i] = ((unsigned long long)i << 32) | v;
+}
+
+__device__ __forceinline__ void bq_push(const LevelParams& p, BlockQueue& bq, uint32_t slot,
+                                        uint32_t v) {
+  const uint32_t pos = atomicAdd(&bq.count, 1u);
+  if (pos < BQ_CAP)
+    bq.items[pos] = v;
+  else
+    enqueue_global(p, slot, v);
+}
+
+// Compacts the block's staged vertices into the global queue with one
+// atomicAdd per block: per-item segment counts, block-wide exclusive scan.
+__device__ void flush_block_queue(const LevelParams& p, BlockQueue& bq, uint32_t slot) {
+  __syncthreads();
+  const uint32_t n = min(bq.count, (uint32_t)BQ_CAP);
+  if (n == 0) return;  // uniform: read after the barrier
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t per = (n + LEVEL_BLOCK - 1) / LEVEL_BLOCK;
+  const uint32_t b = min(n, tid * per), e = min(n, b + per);
+  uint32_t mine = 0;
+  unsigned long long edges = 0;
+  for (uint32_t i = b; i < e; ++i) {
+    const uint32_t v = bq.items[i];
+    const uint32_t deg = p.out_off[v + 1] - p.out_off[v];
+    mine += nseg_of(deg, p.seg);
+    edges += deg;
+  }
+  uint32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= (uint32_t)o) incl += t;
+  }
+  unsigned long long esum = edges;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL, esum, o);
+  if (lane == 31) bq.warp_sum[warp] = incl;
+  if (lane == 0) bq.warp_edges[warp] = esum;
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t run = 0;
+    unsigned long long etot = 0;
+    for (int w = 0; w < LEVEL_BLOCK / 32; ++w) {
+      uint32_t t = bq.warp_sum[w];
+      bq.warp_sum[w] = run;
+      run += t;
+      etot += bq.warp_edges[w];
+    }
+    bq.base = atomicAdd(&p.ctl->qcount[slot], run);
+    atomicAdd(&p.ctl->qverts[slot], n);
+    atomicAdd(&p.ctl->qedges[slot], etot);
+  }
+  __syncthreads();
+  uint32_t pos = bq.base + bq.warp_sum[warp] + incl - mine;
+  unsigned long long* Q = p.Q[slot];
+  for (uint32_t i = b; i < e; ++i) {
+    const uint32_t v = bq.items[i];
+    const uint32_t deg = p.out_off[v + 1] - p.out_off[v];
+    const uint32_t ns = nseg_of(deg, p.seg);
+    for (uint32_t s = 0; s < ns; ++s) Q[pos++] = ((unsigned long long)s << 32) | v;
+  }
+}
+
+// Records distance d for the `newly` lanes of words [k0, k0+VEC) of vertex v.
+// Bottom-up steps own their vertex (plain read-modify-write); top-down steps
+// race with other blocks on the same words (atomicOr; the lanes are disjoint).
+template <int VEC, bool ATOMIC>
+__device__ __forceinline__ void record_level(const LevelParams& p, uint32_t v, uint32_t k0,
+                                             const Words<VEC>& newly, uint32_t d) {
+  const size_t VW = (size_t)p.V * p.W;
+  const size_t off = (size_t)v * p.W + k0;
+  if (d < (1u << p.NP)) {
+    for (uint32_t b = 0; b < p.NP; ++b) {
+      if (!((d >> b) & 1u)) continue;
+      uint32_t* pb = p.planes + b * VW + off;
+      if constexpr (ATOMIC) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+          if (newly.w[j]) atomicOr(pb + j, newly.w[j]);
+      } else {
+        Words<VEC> x = ld_words<VEC>(pb);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) x.w[j] |= newly.w[j];
+        st_words<VEC>(pb, x);
+      }
+    }
+  } else {
+    // Deeper than the planes can encode: mark the lanes and write the rows.
+    uint32_t* dist = p.desc->dist;  // null when only reachability is wanted
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+      uint32_t bits = newly.w[j];
+      if (!bits) continue;
+      atomicOr(p.ovf + off + j, bits);
+      while (dist && bits) {
+        const uint32_t t = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const size_t s = (size_t)(k0 + j) * 32 + t;
+        dist[s * p.V + v] = d;
+      }
+    }
+  }
+}
+
+struct LevelCounters {
+  unsigned long long active = 0, edges = 0, newv = 0, pairs = 0;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t lane_word_mask(uint32_t P, uint32_t k) {
+  const uint32_t lo = k * 32;
+  if (P <= lo) return 0;
+  const uint32_t rem = P - lo;
+  return rem >= 32 ? FULL : ((1u << rem) - 1);
+}
+
+// Bottom-up step over all vertices. A group of LPV lanes owns one vertex; each
+// lane holds VEC of its W words. In-neighbours are gathered CH at a time
+// (CH independent 16-byte loads in flight per lane) and the scan stops once
+// the candidate words cover every still-unvisited lane. Vertices with
+// in-degree >= heavy are scanned by the whole warp afterwards.
+template <int W>
+__device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
+                           LevelCounters& cnt) {
+  using G = Geo<W>;
+  constexpr int VEC = G::VEC, LPV = G::LPV, GPW = G::GPW;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lig = lane % LPV;
+  const uint32_t gbase = lane - lig;
+  const uint32_t gid = lane / LPV;
+  const uint32_t gmask = (LPV == 32) ? FULL : (((1u << LPV) - 1u) << gbase);
+  const uint32_t k0 = lig * VEC;
+  const uint32_t P = p.desc->num_sources;
+  Words<VEC> lmask;
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) lmask.w[j] = lane_word_mask(P, k0 + j);
+  const uint32_t d = L + 1;
+  const uint32_t so = (L + 1) % 3;
+  const uint32_t* __restrict__ Fin = p.F[L % 3];
+  uint32_t* __restrict__ Fout = p.F[so];
+  const uint32_t* __restrict__ in_off = p.in_off;
+  const uint32_t* __restrict__ in_idx = p.in_idx;
+  const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ntiles = (p.V + GPW - 1) / GPW;
+
+  for (uint32_t tile = warp_g; tile < ntiles; tile += nwarps) {
+    const uint32_t v = tile * GPW + gid;
+    uint32_t beg = 0, end = 0;
+    if (v < p.V) {
+      beg = __ldg(in_off + v);
+      end = __ldg(in_off + v + 1);
+    }
+    Words<VEC> needed, visw, cand;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) needed.w[j] = visw.w[j] = cand.w[j] = 0;
+    if (end > beg) {
+      visw = ld_words<VEC>(p.vis + (size_t)v * W + k0);
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) needed.w[j] = ~visw.w[j] & lmask.w[j];
+    }
+    const bool need = (__ballot_sync(FULL, any_bits<VEC>(needed)) & gmask) != 0;
+    const bool heavy = need && (end - beg) >= p.heavy;
+    if (lig == 0 && end > beg) cnt.active += 1;
+
+    if (need && !heavy) {
+      for (uint32_t e0 = beg; e0 < end; e0 += CH) {
+        uint32_t u[CH];
+        if constexpr (LPV >= CH) {
+          const uint32_t mine = (lig < CH && e0 + lig < end) ? __ldg(in_idx + e0 + lig) : FULL;
+#pragma unroll
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(gmask, mine, gbase + j);
+        } else {
+#pragma unroll
+          for (int j = 0; j < CH; ++j) u[j] = (e0 + j < end) ? __ldg(in_idx + e0 + j) : FULL;
+        }
+        Words<VEC> f[CH];
+        if (lig == 0) cnt.edges += min((uint32_t)CH, end - e0);
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          if (u[j] != FULL) {
+            f[j] = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
+          } else {
+#pragma unroll
+            for (int q = 0; q < VEC; ++q) f[j].w[q] = 0;
+          }
+        }
+        bool sat = true;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          uint32_t c = cand.w[q];
+#pragma unroll
+          for (int j = 0; j < CH; ++j) c |= f[j].w[q];
+          cand.w[q] = c;
+          sat &= (c & needed.w[q]) == needed.w[q];
+        }
+        if (__ballot_sync(gmask, !sat) == 0) break;
+      }
+    }
+
+    // Heavy vertices of this tile: the whole warp scans one at a time, each
+    // group taking CH-parent chunks, OR-reduced across groups every round.
+    uint32_t hmask = __ballot_sync(FULL, heavy && lig == 0);
+    while (hmask) {
+      const uint32_t hl = __ffs(hmask) - 1;
+      hmask &= hmask - 1;
+      const uint32_t hbeg = __shfl_sync(FULL, beg, hl);
+      const uint32_t hend = __shfl_sync(FULL, end, hl);
+      Words<VEC> hneed, hc;
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) {
+        hneed.w[q] = __shfl_sync(FULL, needed.w[q], hl + lig);
+        hc.w[q] = 0;
+      }
+      for (uint32_t base = hbeg; base < hend; base += GPW * CH) {
+        const uint32_t e0 = base + gid * CH;
+        if (lig == 0 && e0 < hend) cnt.edges += min((uint32_t)CH, hend - e0);
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          if (e0 + j < hend) {
+            const uint32_t u = __ldg(in_idx + e0 + j);
+            Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
+#pragma unroll
+            for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
+          }
+        }
+        bool sat = true;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          uint32_t c = hc.w[q];
+#pragma unroll
+          for (int o = LPV; o < 32; o <<= 1) c |= __shfl_xor_sync(FULL, c, o);
+          hc.w[q] = c;
+          sat &= (c & hneed.w[q]) == hneed.w[q];
+        }
+        if (__all_sync(FULL, sat)) break;
+      }
+      if (gbase == hl) cand = hc;
+    }
+
+    Words<VEC> newly;
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) newly.w[q] = cand.w[q] & needed.w[q];
+    const bool any_new = (__ballot_sync(FULL, any_bits<VEC>(newly)) & gmask) != 0;
+    if (any_new) {
+      Words<VEC> nv;
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) {
+        nv.w[q] = visw.w[q] | newly.w[q];
+        cnt.pairs += __popc(newly.w[q]);
+      }
+      if (lig == 0) cnt.newv += 1;
+      st_words<VEC>(p.vis + (size_t)v * W + k0, nv);
+      st_words<VEC>(Fout + (size_t)v * W + k0, newly);
+      record_level<VEC, false>(p, v, k0, newly, d);
+      if (lig == 0) bq_push(p, bq, so, v);
+    }
+  }
+}
+
+// Top-down step over the frontier queue. A group takes one queue entry (a
+// vertex and a slice of at most `seg` out-edges) and walks its edges; lanes
+// that hit the same visited word in the same step (frequent when many
+// frontier vertices share a hub) are merged into one atomicOr by the first
+// of them, which then owns the follow-up writes for that word.
+template <int W>
+__device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
+                           LevelCounters& cnt) {
+  using G = Geo<W>;
+  constexpr int VEC = G::VEC, LPV = G::LPV, GPW = G::GPW;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lig = lane % LPV;
+  const uint32_t gbase = lane - lig;
+  const uint32_t gmask = (LPV == 32) ? FULL : (((1u << LPV) - 1u) << gbase);
+  const uint32_t k0 = lig * VEC;
+  const uint32_t d = L + 1;
+  const uint32_t si = L % 3, so = (L + 1) % 3;
+  const uint32_t* __restrict__ Fin = p.F[si];
+  uint32_t* __restrict__ Fout = p.F[so];
+  const unsigned long long* __restrict__ Qi = p.Q[si];
+  const uint32_t nin = *(volatile uint32_t*)&p.ctl->qcount[si];
+  const uint32_t group_g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GPW + lane / LPV;
+  const uint32_t ngroups = ((gridDim.x * blockDim.x) >> 5) * GPW;
+
+  for (uint32_t i = group_g; i < nin; i += ngroups) {
+    const unsigned long long ent = Qi[i];
+    const uint32_t u = (uint32_t)ent;
+    const uint32_t sg = (uint32_t)(ent >> 32);
+    const Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
+    const uint32_t ob = __ldg(p.out_off + u), oe = __ldg(p.out_off + u + 1);
+    const uint32_t eb = ob + sg * p.seg;
+    const uint32_t ee = min(oe, eb + p.seg);
+    if (lig == 0) cnt.edges += ee - eb;
+    for (uint32_t e = eb; e < ee; ++e) {
+      const uint32_t v = __ldg(p.out_idx + e);
+      uint32_t* vrow = p.vis + (size_t)v * W + k0;
+      const Words<VEC> vw = ldcg_words<VEC>(vrow);
+      bool found = false;
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) {
+        const uint32_t needed = f.w[q] & ~vw.w[q];
+        if (needed) {
+          const unsigned act = __activemask();
+          const unsigned peers = __match_any_sync(act, (unsigned long long)(vrow + q));
+          const uint32_t agg = __reduce_or_sync(peers, needed);
+          const uint32_t leader = __ffs(peers) - 1;
+          uint32_t prev = 0;
+          if (lane == leader) prev = atomicOr(vrow + q, agg);
+          prev = __shfl_sync(peers, prev, leader);
+          const uint32_t nw = agg & ~prev;
+          if (lane == leader && nw) {
+            atomicOr(Fout + (size_t)v * W + k0 + q, nw);
+            Words<1> one;
+            one.w[0] = nw;
+            record_level<1, true>(p, v, k0 + q, one, d);
+            cnt.pairs += __popc(nw);
+            found = true;
+          }
+        }
+      }
+      if (__ballot_sync(gmask, found) != 0 && lane == gbase) {
+        if (__ldcg(p.stamp + v) != d && atomicExch(p.stamp + v, d) != d) {
+          bq_push(p, bq, so, v);
+          cnt.newv += 1;
+        }
+      }
+    }
+  }
+}
+
+// Device-side level controller, run by the last block of each level.
+__device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, uint32_t L,
+                           uint32_t dir) {
+  volatile LevelCtl* c = p.ctl;
+  const uint32_t so = (L + 1) % 3;
+  const uint32_t n_next = c->qverts[so];
+  const unsigned long long m_next = c->qedges[so];
+  if (L < LOG_CAP) {
+    LevelRec r;
+    r.level = L;
+    r.dir = dir;
+    r.frontier_vertices = c->qverts[L % 3];
+    r.frontier_entries = c->qcount[L % 3];
+    r.active = c->c_active;
+    r.edges = c->c_edges;
+    r.new_vertices = c->c_newv;
+    r.new_pairs = c->c_pairs;
+    r.t_start = c->t_start;
+    r.t_end = globaltimer();
+    p.log[L] = r;
+  }
+  c->c_active = 0;
+  c->c_edges = 0;
+  c->c_newv = 0;
+  c->c_pairs = 0;
+  c->t_start = ~0ull;
+  if (dir == DIR_PUSH)
+    c->push_levels = c->push_levels + 1;
+  else
+    c->pull_levels = c->pull_levels + 1;
+  bool stop = false;
+  if (n_next == 0) {
+    stop = true;
+  } else if (L + 1 >= p.max_levels) {
+    c->status = c->status | STATUS_LEVEL_CAP;
+    stop = true;
+  }
+  if (stop) {
+    c->terminated = 1;
+    if (h) cudaGraphSetConditional(h, 0);
+    return;
+  }
+  const unsigned long long explored = c->explored + c->qedges[L % 3];
+  c->explored = explored;
+  uint32_t nd = dir;
+  if (p.mode == MODE_PUSH) {
+    nd = DIR_PUSH;
+  } else if (p.mode == MODE_PULL) {
+    nd = DIR_PULL;
+  } else if (dir == DIR_PUSH) {
+    // Beamer's rule: go bottom-up once the frontier's out-edges exceed the
+    // unexplored edges / alpha.
+    const unsigned long long unexplored = p.E > explored ? p.E - explored : 0ull;
+    if (m_next * (unsigned long long)p.alpha > unexplored) nd = DIR_PULL;
+  } else {
+    // Back to top-down once the frontier holds fewer than V / beta vertices.
+    if ((unsigned long long)n_next * p.beta < p.V) nd = DIR_PUSH;
+  }
+  const uint32_t sc = (L + 2) % 3;  // slot of level L-1, becomes level L+2
+  c->qcount[sc] = 0;
+  c->qverts[sc] = 0;
+  c->qedges[sc] = 0;
+  c->dir = nd;
+  c->level = L + 1;
+  c->done_blocks = 0;
+  __threadfence();
+  if (h) cudaGraphSetConditional(h, 1);
+}
+
+template <int W>
+__global__ void __launch_bounds__(LEVEL_BLOCK)
+    level_kernel(LevelParams p, cudaGraphConditionalHandle h) {
+  __shared__ BlockQueue bq;
+  __shared__ unsigned long long s_red[4][LEVEL_BLOCK / 32];
+  __shared__ uint32_t s_last;
+  volatile LevelCtl* c = p.ctl;
+  if (c->terminated) return;  // speculative launches of the host-driven loop
+  const uint32_t L = c->level;
+  const uint32_t dir = c->dir;
+  if (threadIdx.x == 0) {
+    bq.count = 0;
+    atomicMin(&p.ctl->t_start, globaltimer());
+  }
+  __syncthreads();
+
+  // Clear the frontier words of level L-1 (not read or written this level).
+  {
+    const uint32_t sc = (L + 2) % 3;
+    const uint32_t n = c->qcount[sc];
+    const unsigned long long* Qc = p.Q[sc];
+    uint32_t* Fc = p.F[sc];
+    const size_t total = (size_t)n * W;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const unsigned long long ent = Qc[i / W];
+      if ((ent >> 32) == 0) Fc[(size_t)(uint32_t)ent * W + i % W] = 0;
+    }
+  }
+
+  LevelCounters cnt;
+  if (dir == DIR_PULL)
+    pull_phase<W>(p, bq, L, cnt);
+  else
+    push_phase<W>(p, bq, L, cnt);
+  flush_block_queue(p, bq, (L + 1) % 3);
+
+  unsigned long long vals[4] = {cnt.active, cnt.edges, cnt.newv, cnt.pairs};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vals[i] += __shfl_xor_sync(FULL, vals[i], o);
+    if ((threadIdx.x & 31) == 0) s_red[i][threadIdx.x >> 5] = vals[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 4; ++i)
+      for (int w = 0; w < LEVEL_BLOCK / 32; ++w) tot[i] += s_red[i][w];
+    if (tot[0]) atomicAdd(&p.ctl->c_active, tot[0]);
+    if (tot[1]) atomicAdd(&p.ctl->c_edges, tot[1]);
+    if (tot[2]) atomicAdd(&p.ctl->c_newv, tot[2]);
+    if (tot[3]) {
+      atomicAdd(&p.ctl->c_pairs, tot[3]);
+      atomicAdd(&p.ctl->pairs, tot[3]);
+    }
+    __threadfence();
+    const uint32_t prev = atomicAdd(&p.ctl->done_blocks, 1u);
+    s_last = (prev == gridDim.x - 1);
+    if (s_last) {
+      __threadfence();
+      controller(p, h, L, dir);
+    }
+  }
+}
+
+// Level-0 frontier: lane i of word i/32 at vertex sources[i]. Duplicate
+// sources share a vertex and are merged by atomicOr; the vertex is enqueued
+// once (stamp 0).
+template <int W>
+__global__ void init_kernel(LevelParams p) {
+  const PassDesc* dsc = p.desc;
+  const uint32_t P = dsc->num_sources;
+  unsigned long long ok = 0;
+  for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+    const uint32_t s = dsc->sources[i];
+    if (s >= p.V) {
+      atomicOr(&p.ctl->status, STATUS_BAD_SOURCE);
+      continue;
+    }
+    const uint32_t bit = 1u << (i & 31);
+    const size_t w = (size_t)s * W + (i >> 5);
+    atomicOr(p.vis + w, bit);
+    atomicOr(p.F[0] + w, bit);
+    if (atomicExch(p.stamp + s, 0u) != 0u) enqueue_global(p, 0, s);
+    ++ok;
+  }
+  if (ok) atomicAdd(&p.ctl->pairs, ok);
+  if (threadIdx.x == 0) {
+    p.ctl->dir = (p.mode == MODE_PULL) ? DIR_PULL : DIR_PUSH;
+    p.ctl->t_start = ~0ull;
+  }
+}
+
+__device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __clz(x) : 0; }
+
+// Turns visited words + level planes into the source-major u32 distance rows
+// (or copies the visited words out as a reachability bitmask), and zeroes the
+// words it read so the next pass starts from clean buffers. A block stages a
+// tile of 32 vertices x MAT_KC words in shared memory; each warp then writes
+// whole 128-byte row segments dist[s][v0 .. v0+31].
+template <int W>
+__global__ void __launch_bounds__(MAT_BLOCK) materialize_kernel(LevelParams p) {
+  extern __shared__ uint32_t sm[];
+  constexpr int KC = W < MAT_KC ? W : MAT_KC;
+  constexpr int PITCH = KC + 1;
+  const PassDesc* dsc = p.desc;
+  const uint32_t P = dsc->num_sources;
+  const uint32_t Wu = (P + 31) / 32;
+  const uint32_t dmax = p.ctl->level;
+  const uint32_t npu = min(p.NP, bit_length(dmax));
+  const bool use_ovf = dmax >= (1u << p.NP);
+  const size_t VW = (size_t)p.V * W;
+  uint32_t* vs = sm;                    // [32][PITCH]
+  uint32_t* os = vs + 32 * PITCH;       // [32][PITCH]
+  uint32_t* ps = os + 32 * PITCH;       // [npu][32][PITCH]
+  uint32_t* dist = dsc->dist;
+  uint32_t* reach = dsc->reach;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nwarp = blockDim.x >> 5;
+  const uint32_t ntiles = (p.V + 31) / 32;
+
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t v0 = tile * 32;
+    for (uint32_t kb = 0; kb < Wu; kb += KC) {
+      const uint32_t kc = min((uint32_t)KC, Wu - kb);
+      for (uint32_t i = threadIdx.x; i < 32 * kc; i += blockDim.x) {
+        const uint32_t r = i / kc, cc = i % kc, v = v0 + r;
+        uint32_t x = 0, o = 0;
+        if (v < p.V) {
+          const size_t a = (size_t)v * W + kb + cc;
+          x = p.vis[a];
+          p.vis[a] = 0;
+          if (use_ovf) {
+            o = p.ovf[a];
+            p.ovf[a] = 0;
+          }
+          for (uint32_t b = 0; b < npu; ++b) {
+            ps[(b * 32 + r) * PITCH + cc] = p.planes[b * VW + a];
+            p.planes[b * VW + a] = 0;
+          }
+          if (reach) reach[(size_t)v * dsc->reach_wpv + dsc->reach_col + kb + cc] = x;
+        }
+        vs[r * PITCH + cc] = x;
+        os[r * PITCH + cc] = o;
+      }
+      __syncthreads();
+      if (!reach) {
+        const uint32_t v = v0 + lane;
+        const uint32_t s_end = min(P, (kb + kc) * 32);
+        for (uint32_t s = kb * 32 + warp; s < s_end; s += nwarp) {
+          const uint32_t cc = (s >> 5) - kb, j = s & 31;
+          const uint32_t x = vs[lane * PITCH + cc];
+          uint32_t val = DIST_MAX;
+          bool write = v < p.V;
+          if ((x >> j) & 1u) {
+            if (use_ovf && ((os[lane * PITCH + cc] >> j) & 1u)) {
+              write = false;  // written directly by the level kernel
+            } else {
+              val = 0;
+              for (uint32_t b = 0; b < npu; ++b)
+                val |= ((ps[(b * 32 + lane) * PITCH + cc] >> j) & 1u) << b;
+            }
+          }
+          if (write) dist[(size_t)s * p.V + v] = val;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Zeroes the last frontier (level L_end) after the loop has stopped.
+template <int W>
+__global__ void cleanup_kernel(LevelParams p) {
+  const uint32_t L = p.ctl->level;
+  const uint32_t sl = L % 3;
+  const uint32_t n = p.ctl->qcount[sl];
+  const unsigned long long* Qs = p.Q[sl];
+  uint32_t* Fs = p.F[sl];
+  const size_t total = (size_t)n * W;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long ent = Qs[i / W];
+    if ((ent >> 32) == 0) Fs[(size_t)(uint32_t)ent * W + i % W] = 0;
+  }
+}
+
+// Traversed edges of a distance matrix (crates/cli/src/bench.rs:478-491).
+__global__ void traversed_edges_kernel(uint32_t V, const uint32_t* __restrict__ off,
+                                       const uint32_t* __restrict__ dist, uint32_t S,
+                                       unsigned long long* out) {
+  unsigned long long acc = 0;
+  const size_t total = (size_t)S * V;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    if (dist[i] != DIST_MAX) {
+      const uint32_t v = (uint32_t)(i % V);
+      acc += __ldg(off + v + 1) - __ldg(off + v);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+// ------------------------------------------------------------------ host side
+
+template <int W>
+static void fill_info(int num_sms, LevelKernelInfo* k) {
+  k->init = (void*)init_kernel<W>;
+  k->level = (void*)level_kernel<W>;
+  k->materialize = (void*)materialize_kernel<W>;
+  k->cleanup = (void*)cleanup_kernel<W>;
+  k->level_block = LEVEL_BLOCK;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, level_kernel<W>, LEVEL_BLOCK, 0);
+  if (occ < 1) occ = 1;
+  k->level_grid = num_sms * occ;
+  k->mat_block = MAT_BLOCK;
+  constexpr int KC = W < MAT_KC ? W : MAT_KC;
+  // vis + ovf + up to 32 planes, each [32][KC+1] u32
+  k->mat_smem = (size_t)(2 + 32) * 32 * (KC + 1) * sizeof(uint32_t);
+  cudaFuncSetAttribute(materialize_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)k->mat_smem);
+  int mocc = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mocc, materialize_kernel<W>, MAT_BLOCK,
+                                                k->mat_smem);
+  if (mocc < 1) mocc = 1;
+  k->mat_grid = num_sms * mocc;
+}
+
+bool level_kernel_info(uint32_t W, int num_sms, LevelKernelInfo* out) {
+  switch (W) {
+    case 1: fill_info<1>(num_sms, out); return true;
+    case 2: fill_info<2>(num_sms, out); return true;
+    case 4: fill_info<4>(num_sms, out); return true;
+    case 8: fill_info<8>(num_sms, out); return true;
+    case 16: fill_info<16>(num_sms, out); return true;
+    case 32: fill_info<32>(num_sms, out); return true;
+    case 64: fill_info<64>(num_sms, out); return true;
+    default: return false;
+  }
+}
+
+template <int W>
+static void launch_init_t(const LevelParams& p, cudaStream_t s) {
+  init_kernel<W><<<1, 256, 0, s>>>(p);
+}
+void launch_init(const LevelParams& p, cudaStream_t s) {
+  switch (p.W) {
+    case 1: launch_init_t<1>(p, s); break;
+    case 2: launch_init_t<2>(p, s); break;
+    case 4: launch_init_t<4>(p, s); break;
+    case 8: launch_init_t<8>(p, s); break;
+    case 16: launch_init_t<16>(p, s); break;
+    case 32: launch_init_t<32>(p, s); break;
+    case 64: launch_init_t<64>(p, s); break;
+  }
+}
+
+template <int W>
+static void launch_level_t(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
+  level_kernel<W><<<k.level_grid, k.level_block, 0, s>>>(p, (cudaGraphConditionalHandle)0);
+}
+void launch_level(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
+  switch (p.W) {
+    case 1: launch_level_t<1>(p, k, s); break;
+    case 2: launch_level_t<2>(p, k, s); break;
+    case 4: launch_level_t<4>(p, k, s); break;
+    case 8: launch_level_t<8>(p, k, s); break;
+    case 16: launch_level_t<16>(p, k, s); break;
+    case 32: launch_level_t<32>(p, k, s); break;
+    case 64: launch_level_t<64>(p, k, s); break;
+  }
+}
+
+template <int W>
+static void launch_mat_t(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
+  materialize_kernel<W><<<k.mat_grid, k.mat_block, k.mat_smem, s>>>(p);
+}
+void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
+  switch (p.W) {
+    case 1: launch_mat_t<1>(p, k, s); break;
+    case 2: launch_mat_t<2>(p, k, s); break;
+    case 4: launch_mat_t<4>(p, k, s); break;
+    case 8: launch_mat_t<8>(p, k, s); break;
+    case 16: launch_mat_t<16>(p, k, s); break;
+    case 32: launch_mat_t<32>(p, k, s); break;
+    case 64: launch_mat_t<64>(p, k, s); break;
+  }
+}
+
+template <int W>
+static void launch_cleanup_t(const LevelParams& p, cudaStream_t s) {
+  cleanup_kernel<W><<<256, 256, 0, s>>>(p);
+}
+void launch_cleanup(const LevelParams& p, cudaStream_t s) {
+  switch (p.W) {
+    case 1: launch_cleanup_t<1>(p, s); break;
+    case 2: launch_cleanup_t<2>(p, s); break;
+    case 4: launch_cleanup_t<4>(p, s); break;
+    case 8: launch_cleanup_t<8>(p, s); break;
+    case 16: launch_cleanup_t<16>(p, s); break;
+    case 32: launch_cleanup_t<32>(p, s); break;
+    case 64: launch_cleanup_t<64>(p, s); break;
+  }
+}
+
+void launch_traversed_edges(uint32_t V, const uint32_t* off, const uint32_t* dist,
+                            uint32_t num_sources, unsigned long long* out, cudaStream_t s) {
+  cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+  traversed_edges_kernel<<<1024, 256, 0, s>>>(V, off, dist, num_sources, out);
+}
+
+}  // namespace msbfs
