@@ -127,15 +127,15 @@ class ClockSampler:
 def level_bytes(rec, V, W, E):
     """Algorithmic bytes of one level-kernel launch (per-unit figures stated in
     the design doc): bottom-up reads the in-offsets once, the visited row of every
-    vertex with in-edges, (index + W-word frontier row) per in-neighbour
-    gathered, and writes visited + frontier rows of newly reached vertices and
+    vertex with lanes left to discover, an index per in-neighbour examined
+    and a W-word frontier row per in-neighbour in the frontier, and writes visited + frontier rows of newly reached vertices and
     4 bytes per discovered distance; top-down reads its queue entries, the
     offsets + frontier row of each frontier vertex, (index + visited row) per
     out-edge walked, and writes frontier row + queue entry per newly reached
     vertex and 4 bytes per discovered distance."""
     row = 4 * W
     if rec["dir"] == 1:
-        return (4 * (V + 1) + row * rec["active"] + rec["edges"] * (4 + row)
+        return (4 * (V + 1) + row * rec["active"] + rec["edges"] * 4 + rec["rows"] * row
                 + rec["new_vertices"] * 2 * row + 4 * rec["new_pairs"])
     return (8 * rec["frontier_entries"] + rec["frontier_vertices"] * (8 + row)
             + rec["edges"] * (4 + row) + rec["new_vertices"] * (row + 8)
@@ -230,7 +230,10 @@ def run_ours(args, spec):
     src = m.sample_sources(g, S, spec["seed"] + 7919 * rank, min_degree=1)
     V = g.num_vertices
     eng = m.GpuBfsEngine(m.GpuBfsMethod.Auto, device=local)
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the engine launches on it, the CUDA events below are
+    # recorded on it (handle 0 would mean the engine's own stream).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
     eng.upload(g)
     out = torch.empty(S * V, dtype=torch.int32, device="cuda")

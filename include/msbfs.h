@@ -110,6 +110,8 @@ typedef struct msbfs_level_record {
                                  top-down: out-edges walked                */
   uint64_t new_vertices;      /* vertices that gained a visited lane       */
   uint64_t new_pairs;         /* (source, vertex) pairs discovered         */
+  uint64_t rows;              /* bottom-up: frontier rows gathered (the
+                                 in-neighbour was in the frontier)         */
   double device_ms;           /* %globaltimer span of the launch           */
   double event_ms;            /* CUDA-event span (profiling level 2) or 0  */
 } msbfs_level_record;

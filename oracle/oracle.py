@@ -21,7 +21,12 @@ _lib = None
 
 
 def build() -> Path:
-    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    import platform
+    stamp = HERE / "_build" / "arch.txt"
+    arch = platform.machine()
+    force = not stamp.exists() or stamp.read_text().strip() != arch
+    subprocess.run(["make", "-s", "-C", str(HERE)] + (["-B"] if force else []), check=True)
+    stamp.write_text(arch + "\n")
     return LIB
 
 

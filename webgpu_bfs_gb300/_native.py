@@ -47,6 +47,7 @@ class LevelRecord(C.Structure):
         ("edges", C.c_uint64),
         ("new_vertices", C.c_uint64),
         ("new_pairs", C.c_uint64),
+        ("rows", C.c_uint64),
         ("device_ms", C.c_double),
         ("event_ms", C.c_double),
     ]

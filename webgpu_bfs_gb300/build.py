@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import subprocess
 import sys
 from pathlib import Path
@@ -65,6 +66,11 @@ def _compile(src: Path, obj: Path, verbose: bool) -> None:
 def build_native(verbose: bool = False, force: bool = False) -> Path:
     """Builds (if needed) and returns the path of libmsbfs.so."""
     OBJDIR.mkdir(parents=True, exist_ok=True)
+    # Objects built on another host architecture are never reused.
+    stamp = LIBDIR / "arch.txt"
+    arch = platform.machine()
+    if not stamp.exists() or stamp.read_text().strip() != arch:
+        force = True
     sources = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     newest_header = max((h.stat().st_mtime for h in _headers()), default=0.0)
     jobs = []
@@ -90,6 +96,7 @@ def build_native(verbose: bool = False, force: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    stamp.write_text(arch + "\n")
     return LIB
 
 

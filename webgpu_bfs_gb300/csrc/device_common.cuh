@@ -35,6 +35,7 @@ struct LevelRec {
   unsigned long long edges;    // bottom-up: in-neighbour gathers; top-down: out-edges walked
   unsigned long long new_vertices;
   unsigned long long new_pairs;
+  unsigned long long rows;     // frontier rows gathered (bottom-up)
   unsigned long long t_start;
   unsigned long long t_end;
 };
@@ -59,7 +60,24 @@ struct LevelCtl {
   unsigned long long c_edges;
   unsigned long long c_newv;
   unsigned long long c_pairs;
+  unsigned long long c_rows;
   unsigned long long t_start;    // min %globaltimer over the level's blocks
+  uint32_t work;                 // vertex-tile cursor of the running bottom-up step
+  uint32_t use_bits;             // bottom-up step checks frontier bitmaps first
+
+  // Source lanes whose frontier is non-empty: lanes[L & 1] for the level being
+  // expanded, lanes[(L + 1) & 1] collects the lanes that gain vertices. A lane
+  // with an empty frontier can discover nothing, so bottom-up steps ignore it.
+  uint32_t lanes[2][64];
+};
+
+// One slice of a high in-degree vertex's in-edge list, scanned by one warp
+// during bottom-up steps; the last slice to finish records the result.
+struct HeavyChunk {
+  uint32_t v;      // vertex
+  uint32_t j;      // slice index
+  uint32_t nch;    // slices of this vertex
+  uint32_t h;      // index of the vertex among heavy vertices
 };
 
 // Per-pass descriptor, read from device memory so one captured CUDA graph can
@@ -88,6 +106,7 @@ struct LevelParams {
   uint32_t* ovf;
   unsigned long long* Q[3];
   uint32_t* stamp;
+  uint32_t* fbits[3];  // frontier membership bitmaps (V bits), rotated like F
   LevelCtl* ctl;
   LevelRec* log;      // LOG_CAP records
   const PassDesc* desc;
@@ -99,6 +118,12 @@ struct LevelParams {
   uint32_t seg;       // out-edges per queue entry
   uint32_t heavy;     // in-degree from which a whole warp scans one vertex
   uint32_t max_levels;
+  uint32_t split;     // in-degree above which in-edges are sliced across warps
+  uint32_t n_hchunks;
+  const HeavyChunk* hchunks;
+  uint32_t* hcand;    // [n_heavy][W] candidate words of sliced vertices
+  uint32_t* hcount;   // [n_heavy] slices finished this level
+  uint32_t bits_div;  // bitmap check when the frontier holds < V / bits_div vertices
 };
 
 // Launch helpers implemented in level_kernels.cu / cta_kernel.cu.

@@ -47,6 +47,11 @@ struct msbfs_graph {
   uint32_t* idx = nullptr;
   uint32_t* coff = nullptr;  // CSC (== CSR when symmetric)
   uint32_t* cidx = nullptr;
+  // In-edge lists longer than `split` are cut into slices for bottom-up steps.
+  uint32_t split = 0;
+  uint32_t n_heavy = 0;
+  uint32_t n_hchunks = 0;
+  HeavyChunk* hchunks = nullptr;
 };
 
 namespace {
@@ -114,7 +119,9 @@ struct msbfs_engine {
   uint32_t alpha = 14;
   uint32_t beta = 24;
   uint32_t seg = 64;
-  uint32_t heavy = 64;
+  uint32_t heavy = 32;
+  uint32_t split = 256;
+  uint32_t bits_div = 64;
   bool host_loop = false;
   int profiling = 0;
   std::vector<msbfs_level_record> log;       // records of the last call
@@ -208,6 +215,15 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w) {
   m2.height = 1;
   m2.pitch = (size_t)w->p.V * 4;
   CK(cudaGraphAddMemsetNode(&n_mst, g, nullptr, 0, &m2));
+  cudaGraphNode_t n_mfb;
+  cudaMemsetParams m3{};
+  m3.dst = w->p.fbits[0];
+  m3.value = 0;
+  m3.elementSize = 4;
+  m3.width = 3 * (((size_t)w->p.V + 31) / 32);
+  m3.height = 1;
+  m3.pitch = m3.width * 4;
+  CK(cudaGraphAddMemsetNode(&n_mfb, g, nullptr, 0, &m3));
 
   void* args_p[] = {&w->p};
   cudaKernelNodeParams ki{};
@@ -216,8 +232,8 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w) {
   ki.blockDim = dim3(256);
   ki.sharedMemBytes = 0;
   ki.kernelParams = args_p;
-  cudaGraphNode_t deps_init[2] = {n_mctl, n_mst};
-  CK(cudaGraphAddKernelNode(&n_init, g, deps_init, 2, &ki));
+  cudaGraphNode_t deps_init[3] = {n_mctl, n_mst, n_mfb};
+  CK(cudaGraphAddKernelNode(&n_init, g, deps_init, 3, &ki));
 
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
@@ -293,7 +309,11 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   p.beta = eng->beta;
   p.seg = eng->seg;
   p.heavy = eng->heavy;
+  p.bits_div = eng->bits_div;
   p.max_levels = (uint32_t)std::min<uint64_t>(g->V + 2, 0xFFFFFFF0ull);
+  p.split = g->split;
+  p.n_hchunks = g->n_hchunks;
+  p.hchunks = g->hchunks;
   int rc;
   void* ptr;
   if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4))) return rc;
@@ -312,6 +332,9 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   }
   if ((rc = dev_alloc(eng, w.get(), &ptr, g->V * 4))) return rc;
   p.stamp = (uint32_t*)ptr;
+  const size_t fwords = (g->V + 31) / 32;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, 3 * fwords * 4))) return rc;
+  for (int i = 0; i < 3; ++i) p.fbits[i] = (uint32_t*)ptr + i * fwords;
   if ((rc = dev_alloc(eng, w.get(), &ptr, sizeof(LevelCtl)))) return rc;
   w->d_ctl = (LevelCtl*)ptr;
   p.ctl = w->d_ctl;
@@ -321,6 +344,10 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   if ((rc = dev_alloc(eng, w.get(), &ptr, sizeof(LevelRec) * LOG_CAP))) return rc;
   w->d_log = (LevelRec*)ptr;
   p.log = w->d_log;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)g->n_heavy * W * 4))) return rc;
+  p.hcand = (uint32_t*)ptr;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)g->n_heavy * 4))) return rc;
+  p.hcount = (uint32_t*)ptr;
   if (!eng->host_loop) {
     rc = build_graph_exec(eng, w.get());
     if (rc) {
@@ -353,6 +380,7 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
   int rc;
   CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
   CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
+  CK(cudaMemsetAsync(w->p.fbits[0], 0, 3 * ((w->p.V + 31) / 32) * sizeof(uint32_t), eng->stream));
   launch_init(w->p, eng->stream);
   LevelCtl probe{};
   ms->clear();
@@ -385,6 +413,7 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
 int run_pass_host_loop(msbfs_engine* eng, Workspace* w) {
   CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
   CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
+  CK(cudaMemsetAsync(w->p.fbits[0], 0, 3 * ((w->p.V + 31) / 32) * sizeof(uint32_t), eng->stream));
   launch_init(w->p, eng->stream);
   LevelCtl probe{};
   for (uint64_t launched = 0;;) {
@@ -607,6 +636,7 @@ int finish_call(msbfs_engine* eng, msbfs_stats* stats) {
         o.edges = r.edges;
         o.new_vertices = r.new_vertices;
         o.new_pairs = r.new_pairs;
+        o.rows = r.rows;
         o.device_ms = r.t_end > r.t_start ? (double)(r.t_end - r.t_start) * 1e-6 : 0.0;
         o.event_ms = (ev && L < ev->size() && !ev->empty()) ? (*ev)[L] : 0.0;
         eng->log.push_back(o);
@@ -657,6 +687,25 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
     CK(cudaMemcpy(g->coff, t.off.data(), (V + 1) * 4, cudaMemcpyHostToDevice));
     if (E) CK(cudaMemcpy(g->cidx, t.idx.data(), E * 4, cudaMemcpyHostToDevice));
   }
+  // Slice table of long in-edge lists (in-degree = CSC row length).
+  g->split = eng->split;
+  std::vector<HeavyChunk> chunks;
+  for (size_t v = 0; v < V; ++v) {
+    const uint32_t indeg = t.off[v + 1] - t.off[v];
+    if (indeg <= g->split) continue;
+    const uint32_t nch = (indeg + g->split - 1) / g->split;
+    for (uint32_t j = 0; j < nch; ++j) chunks.push_back(HeavyChunk{(uint32_t)v, j, nch, g->n_heavy});
+    g->n_heavy++;
+  }
+  // Longest lists first so their slices start early in every bottom-up step.
+  std::stable_sort(chunks.begin(), chunks.end(), [](const HeavyChunk& a, const HeavyChunk& b) {
+    return a.nch > b.nch;
+  });
+  g->n_hchunks = (uint32_t)chunks.size();
+  CK(cudaMalloc((void**)&g->hchunks, std::max<size_t>(chunks.size(), 1) * sizeof(HeavyChunk)));
+  if (!chunks.empty())
+    CK(cudaMemcpy(g->hchunks, chunks.data(), chunks.size() * sizeof(HeavyChunk),
+                  cudaMemcpyHostToDevice));
   *out = g.release();
   return MSBFS_OK;
 }
@@ -680,6 +729,7 @@ void free_graph(msbfs_graph* g) {
   }
   cudaFree(g->off);
   cudaFree(g->idx);
+  cudaFree(g->hchunks);
   delete g;
 }
 

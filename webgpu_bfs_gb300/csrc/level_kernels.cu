@@ -242,7 +242,7 @@ __device__ __forceinline__ void record_level(const LevelParams& p, uint32_t v, u
 }
 
 struct LevelCounters {
-  unsigned long long active = 0, edges = 0, newv = 0, pairs = 0;
+  unsigned long long active = 0, edges = 0, newv = 0, pairs = 0, rows = 0;
 };
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -258,13 +258,64 @@ __device__ __forceinline__ uint32_t lane_word_mask(uint32_t P, uint32_t k) {
   return rem >= 32 ? FULL : ((1u << rem) - 1);
 }
 
-// Bottom-up step over all vertices. A group of LPV lanes owns one vertex; each
-// lane holds VEC of its W words. In-neighbours are gathered CH at a time
-// (CH independent 16-byte loads in flight per lane) and the scan stops once
-// the candidate words cover every still-unvisited lane. Vertices with
-// in-degree >= heavy are scanned by the whole warp afterwards.
+// Lane bits of the words [k0, k0+VEC) that are still worth discovering at
+// level L: sources of this pass whose frontier is non-empty.
+template <int VEC>
+__device__ __forceinline__ Words<VEC> alive_lanes(const LevelParams& p, uint32_t L, uint32_t k0) {
+  Words<VEC> m;
+  const uint32_t P = p.desc->num_sources;
+  const volatile uint32_t* lanes = p.ctl->lanes[L & 1];
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) m.w[j] = lane_word_mask(P, k0 + j) & lanes[k0 + j];
+  return m;
+}
+
+// Visited/frontier/level/queue writes for a vertex owned by the calling group
+// (all LPV lanes call it with their own VEC words).
+template <int W, int VEC>
+__device__ __forceinline__ void pull_commit(const LevelParams& p, BlockQueue& bq, uint32_t* s_lanes,
+                                            uint32_t L, uint32_t v, uint32_t k0, uint32_t lig,
+                                            const Words<VEC>& visw, const Words<VEC>& newly,
+                                            LevelCounters& cnt) {
+  Words<VEC> nv;
+#pragma unroll
+  for (int q = 0; q < VEC; ++q) {
+    nv.w[q] = visw.w[q] | newly.w[q];
+    cnt.pairs += __popc(newly.w[q]);
+    if (newly.w[q]) atomicOr(s_lanes + k0 + q, newly.w[q]);
+  }
+  uint32_t* Fout = p.F[(L + 1) % 3];
+  st_words<VEC>(p.vis + (size_t)v * W + k0, nv);
+  st_words<VEC>(Fout + (size_t)v * W + k0, newly);
+  record_level<VEC, false>(p, v, k0, newly, L + 1);
+  if (lig == 0) {
+    cnt.newv += 1;
+    atomicOr(p.fbits[(L + 1) % 3] + (v >> 5), 1u << (v & 31));
+    bq_push(p, bq, (L + 1) % 3, v);
+  }
+}
+
+// With a sparse frontier, checking the 1-bit membership map first avoids most
+// 16-byte row loads; with a dense one the extra dependent load costs more
+// than it saves, so the controller turns the check off (`fb` null).
+__device__ __forceinline__ bool in_frontier(const uint32_t* fb, uint32_t u) {
+  return !fb || ((__ldg(fb + (u >> 5)) >> (u & 31)) & 1u);
+}
+
+constexpr uint32_t TILE_BATCH = 16;  // vertex tiles claimed per cursor bump
+
+// Bottom-up step over all vertices, in two parts.
+// (1) Sliced vertices (in-degree > split): each warp takes one slice of one
+//     vertex's in-edges, ORs the in-neighbours' frontier rows (every group of
+//     the warp takes CH of them per round), publishes the partial candidate
+//     words with atomicOr, and the last slice to arrive commits the vertex.
+// (2) Every other vertex: a group of LPV lanes owns it, each lane holding VEC
+//     of its W words; in-neighbours are gathered CH at a time (CH independent
+//     16-byte loads in flight per lane) and the scan stops once the candidate
+//     words cover every lane still to be discovered. Vertices with in-degree
+//     >= heavy are scanned by the whole warp.
 template <int W>
-__device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
+__device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lanes, uint32_t L,
                            LevelCounters& cnt) {
   using G = Geo<W>;
   constexpr int VEC = G::VEC, LPV = G::LPV, GPW = G::GPW;
@@ -274,26 +325,113 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
   const uint32_t gid = lane / LPV;
   const uint32_t gmask = (LPV == 32) ? FULL : (((1u << LPV) - 1u) << gbase);
   const uint32_t k0 = lig * VEC;
-  const uint32_t P = p.desc->num_sources;
-  Words<VEC> lmask;
-#pragma unroll
-  for (int j = 0; j < VEC; ++j) lmask.w[j] = lane_word_mask(P, k0 + j);
-  const uint32_t d = L + 1;
-  const uint32_t so = (L + 1) % 3;
+  const Words<VEC> lmask = alive_lanes<VEC>(p, L, k0);
   const uint32_t* __restrict__ Fin = p.F[L % 3];
-  uint32_t* __restrict__ Fout = p.F[so];
+  const uint32_t* __restrict__ fb =
+      *(volatile uint32_t*)&p.ctl->use_bits ? p.fbits[L % 3] : nullptr;
   const uint32_t* __restrict__ in_off = p.in_off;
   const uint32_t* __restrict__ in_idx = p.in_idx;
   const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t ntiles = (p.V + GPW - 1) / GPW;
 
-  for (uint32_t tile = warp_g; tile < ntiles; tile += nwarps) {
+  // ---- (1) sliced high in-degree vertices
+  for (uint32_t ci = warp_g; ci < p.n_hchunks; ci += nwarps) {
+    const HeavyChunk hk = p.hchunks[ci];
+    const uint32_t v = hk.v;
+    const uint32_t vb = __ldg(in_off + v);
+    const uint32_t beg = vb + hk.j * p.split;
+    const uint32_t end = min(__ldg(in_off + v + 1), beg + p.split);
+    const Words<VEC> visw = ld_words<VEC>(p.vis + (size_t)v * W + k0);
+    Words<VEC> needed, hc, shared_c;
+    bool sat = true;
+    uint32_t* hrow = p.hcand + (size_t)hk.h * W + k0;
+    shared_c = ldcg_words<VEC>(hrow);
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) {
+      needed.w[q] = ~visw.w[q] & lmask.w[q];
+      hc.w[q] = 0;
+      sat &= (shared_c.w[q] & needed.w[q]) == needed.w[q];
+    }
+    // Every slice of v sees the same `needed` (only the committing slice
+    // writes v's visited row, after all slices arrived).
+    if (!__any_sync(FULL, any_bits<VEC>(needed))) continue;
+    if (hk.j == 0 && lane == 0) cnt.active += 1;
+    if (!__all_sync(FULL, sat)) {
+      for (uint32_t base = beg; base < end; base += GPW * CH) {
+        const uint32_t e0 = base + gid * CH;
+        if (lig == 0 && e0 < end) cnt.edges += min((uint32_t)CH, end - e0);
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          if (e0 + j < end) {
+            const uint32_t u = __ldg(in_idx + e0 + j);
+            if (in_frontier(fb, u)) {
+              if (lig == 0) cnt.rows += 1;
+              Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
+#pragma unroll
+              for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
+            }
+          }
+        }
+        bool s2 = true;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          uint32_t c = hc.w[q];
+#pragma unroll
+          for (int o = LPV; o < 32; o <<= 1) c |= __shfl_xor_sync(FULL, c, o);
+          hc.w[q] = c;
+          s2 &= (c & needed.w[q]) == needed.w[q];
+        }
+        if (__all_sync(FULL, s2)) break;
+      }
+      if (gid == 0) {
+#pragma unroll
+        for (int q = 0; q < VEC; ++q)
+          if (hc.w[q] & needed.w[q]) atomicOr(hrow + q, hc.w[q] & needed.w[q]);
+      }
+    }
+    __threadfence();
+    uint32_t last = 0;
+    if (lane == 0) last = (atomicAdd(p.hcount + hk.h, 1u) == hk.nch - 1) ? 1u : 0u;
+    last = __shfl_sync(FULL, last, 0);
+    if (last) {
+      __threadfence();
+      if (gid == 0) {
+        const Words<VEC> fin = ldcg_words<VEC>(hrow);
+        Words<VEC> newly, zero;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          newly.w[q] = fin.w[q] & needed.w[q];
+          zero.w[q] = 0;
+        }
+        st_words<VEC>(hrow, zero);
+        const bool any_new = (__ballot_sync(gmask, any_bits<VEC>(newly)) & gmask) != 0;
+        if (any_new) pull_commit<W, VEC>(p, bq, s_lanes, L, v, k0, lig, visw, newly, cnt);
+        if (lane == 0) p.hcount[hk.h] = 0;
+      }
+    }
+  }
+
+  // ---- (2) all other vertices
+  // Tiles are claimed dynamically: on power-law graphs the expensive vertices
+  // cluster (R-MAT puts its hubs at low ids), so a static split leaves most
+  // warps idle behind a few.
+  const uint32_t ntiles = (p.V + GPW - 1) / GPW;
+  uint32_t tile = 0, tile_end = 0;
+  for (;;) {
+    if (tile == tile_end) {
+      uint32_t t0 = 0;
+      if (lane == 0) t0 = atomicAdd(&p.ctl->work, TILE_BATCH);
+      tile = __shfl_sync(FULL, t0, 0);
+      if (tile >= ntiles) break;
+      tile_end = min(tile + TILE_BATCH, ntiles);
+    }
     const uint32_t v = tile * GPW + gid;
+    ++tile;
     uint32_t beg = 0, end = 0;
     if (v < p.V) {
       beg = __ldg(in_off + v);
       end = __ldg(in_off + v + 1);
+      if (end - beg > p.split) end = beg;  // sliced: handled in part (1)
     }
     Words<VEC> needed, visw, cand;
 #pragma unroll
@@ -305,7 +443,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
     }
     const bool need = (__ballot_sync(FULL, any_bits<VEC>(needed)) & gmask) != 0;
     const bool heavy = need && (end - beg) >= p.heavy;
-    if (lig == 0 && end > beg) cnt.active += 1;
+    if (lig == 0 && need) cnt.active += 1;
 
     if (need && !heavy) {
       for (uint32_t e0 = beg; e0 < end; e0 += CH) {
@@ -322,7 +460,8 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
         if (lig == 0) cnt.edges += min((uint32_t)CH, end - e0);
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (u[j] != FULL) {
+          if (u[j] != FULL && in_frontier(fb, u[j])) {
+            if (lig == 0) cnt.rows += 1;
             f[j] = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
           } else {
 #pragma unroll
@@ -342,8 +481,6 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
       }
     }
 
-    // Heavy vertices of this tile: the whole warp scans one at a time, each
-    // group taking CH-parent chunks, OR-reduced across groups every round.
     uint32_t hmask = __ballot_sync(FULL, heavy && lig == 0);
     while (hmask) {
       const uint32_t hl = __ffs(hmask) - 1;
@@ -363,9 +500,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
         for (int j = 0; j < CH; ++j) {
           if (e0 + j < hend) {
             const uint32_t u = __ldg(in_idx + e0 + j);
-            Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
+            if (in_frontier(fb, u)) {
+              if (lig == 0) cnt.rows += 1;
+              Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
 #pragma unroll
-            for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
+              for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
+            }
           }
         }
         bool sat = true;
@@ -386,19 +526,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
 #pragma unroll
     for (int q = 0; q < VEC; ++q) newly.w[q] = cand.w[q] & needed.w[q];
     const bool any_new = (__ballot_sync(FULL, any_bits<VEC>(newly)) & gmask) != 0;
-    if (any_new) {
-      Words<VEC> nv;
-#pragma unroll
-      for (int q = 0; q < VEC; ++q) {
-        nv.w[q] = visw.w[q] | newly.w[q];
-        cnt.pairs += __popc(newly.w[q]);
-      }
-      if (lig == 0) cnt.newv += 1;
-      st_words<VEC>(p.vis + (size_t)v * W + k0, nv);
-      st_words<VEC>(Fout + (size_t)v * W + k0, newly);
-      record_level<VEC, false>(p, v, k0, newly, d);
-      if (lig == 0) bq_push(p, bq, so, v);
-    }
+    if (any_new) pull_commit<W, VEC>(p, bq, s_lanes, L, v, k0, lig, visw, newly, cnt);
   }
 }
 
@@ -408,7 +536,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
 // frontier vertices share a hub) are merged into one atomicOr by the first
 // of them, which then owns the follow-up writes for that word.
 template <int W>
-__device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
+__device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lanes, uint32_t L,
                            LevelCounters& cnt) {
   using G = Geo<W>;
   constexpr int VEC = G::VEC, LPV = G::LPV, GPW = G::GPW;
@@ -458,12 +586,14 @@ __device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t L,
             one.w[0] = nw;
             record_level<1, true>(p, v, k0 + q, one, d);
             cnt.pairs += __popc(nw);
+            atomicOr(s_lanes + k0 + q, nw);
             found = true;
           }
         }
       }
       if (__ballot_sync(gmask, found) != 0 && lane == gbase) {
         if (__ldcg(p.stamp + v) != d && atomicExch(p.stamp + v, d) != d) {
+          atomicOr(p.fbits[so] + (v >> 5), 1u << (v & 31));
           bq_push(p, bq, so, v);
           cnt.newv += 1;
         }
@@ -489,6 +619,7 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
     r.edges = c->c_edges;
     r.new_vertices = c->c_newv;
     r.new_pairs = c->c_pairs;
+    r.rows = c->c_rows;
     r.t_start = c->t_start;
     r.t_end = globaltimer();
     p.log[L] = r;
@@ -497,6 +628,7 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
   c->c_edges = 0;
   c->c_newv = 0;
   c->c_pairs = 0;
+  c->c_rows = 0;
   c->t_start = ~0ull;
   if (dir == DIR_PUSH)
     c->push_levels = c->push_levels + 1;
@@ -522,14 +654,15 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
   } else if (p.mode == MODE_PULL) {
     nd = DIR_PULL;
   } else if (dir == DIR_PUSH) {
-    // Beamer's rule: go bottom-up once the frontier's out-edges exceed the
-    // unexplored edges / alpha.
-    const unsigned long long unexplored = p.E > explored ? p.E - explored : 0ull;
-    if (m_next * (unsigned long long)p.alpha > unexplored) nd = DIR_PULL;
+    // Go bottom-up once the frontier's out-edges exceed E / alpha. (Beamer's
+    // unexplored-edge estimate does not apply: with many sources a vertex
+    // sits in the frontier of several levels, so explored edges exceed E.)
+    if (m_next * (unsigned long long)p.alpha > p.E) nd = DIR_PULL;
   } else {
     // Back to top-down once the frontier holds fewer than V / beta vertices.
     if ((unsigned long long)n_next * p.beta < p.V) nd = DIR_PUSH;
   }
+  for (uint32_t k = 0; k < p.W; ++k) c->lanes[L & 1][k] = 0;  // becomes level L+2's collector
   const uint32_t sc = (L + 2) % 3;  // slot of level L-1, becomes level L+2
   c->qcount[sc] = 0;
   c->qverts[sc] = 0;
@@ -537,6 +670,8 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
   c->dir = nd;
   c->level = L + 1;
   c->done_blocks = 0;
+  c->work = 0;
+  c->use_bits = (p.bits_div && (unsigned long long)n_next * p.bits_div < p.V) ? 1u : 0u;
   __threadfence();
   if (h) cudaGraphSetConditional(h, 1);
 }
@@ -545,7 +680,8 @@ template <int W>
 __global__ void __launch_bounds__(LEVEL_BLOCK)
     level_kernel(LevelParams p, cudaGraphConditionalHandle h) {
   __shared__ BlockQueue bq;
-  __shared__ unsigned long long s_red[4][LEVEL_BLOCK / 32];
+  __shared__ unsigned long long s_red[5][LEVEL_BLOCK / 32];
+  __shared__ uint32_t s_lanes[W];
   __shared__ uint32_t s_last;
   volatile LevelCtl* c = p.ctl;
   if (c->terminated) return;  // speculative launches of the host-driven loop
@@ -555,6 +691,7 @@ __global__ void __launch_bounds__(LEVEL_BLOCK)
     bq.count = 0;
     atomicMin(&p.ctl->t_start, globaltimer());
   }
+  for (uint32_t k = threadIdx.x; k < W; k += blockDim.x) s_lanes[k] = 0;
   __syncthreads();
 
   // Clear the frontier words of level L-1 (not read or written this level).
@@ -569,30 +706,37 @@ __global__ void __launch_bounds__(LEVEL_BLOCK)
       const unsigned long long ent = Qc[i / W];
       if ((ent >> 32) == 0) Fc[(size_t)(uint32_t)ent * W + i % W] = 0;
     }
+    uint32_t* fc = p.fbits[sc];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (p.V + 31) / 32;
+         i += gridDim.x * blockDim.x)
+      fc[i] = 0;
   }
 
   LevelCounters cnt;
   if (dir == DIR_PULL)
-    pull_phase<W>(p, bq, L, cnt);
+    pull_phase<W>(p, bq, s_lanes, L, cnt);
   else
-    push_phase<W>(p, bq, L, cnt);
-  flush_block_queue(p, bq, (L + 1) % 3);
+    push_phase<W>(p, bq, s_lanes, L, cnt);
+  flush_block_queue(p, bq, (L + 1) % 3);  // starts with a block barrier
+  for (uint32_t k = threadIdx.x; k < W; k += blockDim.x)
+    if (s_lanes[k]) atomicOr(&p.ctl->lanes[(L + 1) & 1][k], s_lanes[k]);
 
-  unsigned long long vals[4] = {cnt.active, cnt.edges, cnt.newv, cnt.pairs};
+  unsigned long long vals[5] = {cnt.active, cnt.edges, cnt.newv, cnt.pairs, cnt.rows};
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < 5; ++i) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vals[i] += __shfl_xor_sync(FULL, vals[i], o);
     if ((threadIdx.x & 31) == 0) s_red[i][threadIdx.x >> 5] = vals[i];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long tot[4] = {0, 0, 0, 0};
-    for (int i = 0; i < 4; ++i)
+    unsigned long long tot[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 5; ++i)
       for (int w = 0; w < LEVEL_BLOCK / 32; ++w) tot[i] += s_red[i][w];
     if (tot[0]) atomicAdd(&p.ctl->c_active, tot[0]);
     if (tot[1]) atomicAdd(&p.ctl->c_edges, tot[1]);
     if (tot[2]) atomicAdd(&p.ctl->c_newv, tot[2]);
+    if (tot[4]) atomicAdd(&p.ctl->c_rows, tot[4]);
     if (tot[3]) {
       atomicAdd(&p.ctl->c_pairs, tot[3]);
       atomicAdd(&p.ctl->pairs, tot[3]);
@@ -625,6 +769,8 @@ __global__ void init_kernel(LevelParams p) {
     const size_t w = (size_t)s * W + (i >> 5);
     atomicOr(p.vis + w, bit);
     atomicOr(p.F[0] + w, bit);
+    atomicOr(&p.ctl->lanes[0][i >> 5], bit);
+    atomicOr(p.fbits[0] + (s >> 5), 1u << (s & 31));
     if (atomicExch(p.stamp + s, 0u) != 0u) enqueue_global(p, 0, s);
     ++ok;
   }
@@ -640,34 +786,39 @@ __device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __c
 // Turns visited words + level planes into the source-major u32 distance rows
 // (or copies the visited words out as a reachability bitmask), and zeroes the
 // words it read so the next pass starts from clean buffers. A block stages a
-// tile of 32 vertices x MAT_KC words in shared memory; each warp then writes
-// whole 128-byte row segments dist[s][v0 .. v0+31].
+// tile of MAT_TV consecutive vertices x KC words in shared memory (word-major,
+// so a lane reads its 4 vertices with one 16-byte load); warp c then owns word
+// c: it keeps the tile's visited/plane words of its 4 vertices in registers
+// and writes the 32 rows s = 32*(kb+c) + j as 512-byte contiguous segments
+// (one 16-byte store per lane per row).
+constexpr int MAT_TV = 128;
+constexpr int MAT_NPMAX = 8;
+
 template <int W>
 __global__ void __launch_bounds__(MAT_BLOCK) materialize_kernel(LevelParams p) {
-  extern __shared__ uint32_t sm[];
+  extern __shared__ __align__(16) uint32_t sm[];
   constexpr int KC = W < MAT_KC ? W : MAT_KC;
-  constexpr int PITCH = KC + 1;
   const PassDesc* dsc = p.desc;
   const uint32_t P = dsc->num_sources;
   const uint32_t Wu = (P + 31) / 32;
   const uint32_t dmax = p.ctl->level;
-  const uint32_t npu = min(p.NP, bit_length(dmax));
+  const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
   const bool use_ovf = dmax >= (1u << p.NP);
   const size_t VW = (size_t)p.V * W;
-  uint32_t* vs = sm;                    // [32][PITCH]
-  uint32_t* os = vs + 32 * PITCH;       // [32][PITCH]
-  uint32_t* ps = os + 32 * PITCH;       // [npu][32][PITCH]
+  uint32_t* vs = sm;                  // [KC][MAT_TV]
+  uint32_t* os = vs + KC * MAT_TV;    // [KC][MAT_TV]
+  uint32_t* ps = os + KC * MAT_TV;    // [npu][KC][MAT_TV]
   uint32_t* dist = dsc->dist;
   uint32_t* reach = dsc->reach;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t nwarp = blockDim.x >> 5;
-  const uint32_t ntiles = (p.V + 31) / 32;
+  const uint32_t ntiles = (p.V + MAT_TV - 1) / MAT_TV;
+  const bool vec_ok = (p.V % 4 == 0) && (((uintptr_t)dist & 15) == 0);
 
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint32_t v0 = tile * 32;
+    const uint32_t v0 = tile * MAT_TV;
     for (uint32_t kb = 0; kb < Wu; kb += KC) {
       const uint32_t kc = min((uint32_t)KC, Wu - kb);
-      for (uint32_t i = threadIdx.x; i < 32 * kc; i += blockDim.x) {
+      for (uint32_t i = threadIdx.x; i < MAT_TV * kc; i += blockDim.x) {
         const uint32_t r = i / kc, cc = i % kc, v = v0 + r;
         uint32_t x = 0, o = 0;
         if (v < p.V) {
@@ -679,33 +830,57 @@ __global__ void __launch_bounds__(MAT_BLOCK) materialize_kernel(LevelParams p) {
             p.ovf[a] = 0;
           }
           for (uint32_t b = 0; b < npu; ++b) {
-            ps[(b * 32 + r) * PITCH + cc] = p.planes[b * VW + a];
+            ps[(b * KC + cc) * MAT_TV + r] = p.planes[b * VW + a];
             p.planes[b * VW + a] = 0;
           }
           if (reach) reach[(size_t)v * dsc->reach_wpv + dsc->reach_col + kb + cc] = x;
+        } else {
+          for (uint32_t b = 0; b < npu; ++b) ps[(b * KC + cc) * MAT_TV + r] = 0;
         }
-        vs[r * PITCH + cc] = x;
-        os[r * PITCH + cc] = o;
+        vs[cc * MAT_TV + r] = x;
+        os[cc * MAT_TV + r] = o;
       }
       __syncthreads();
-      if (!reach) {
-        const uint32_t v = v0 + lane;
-        const uint32_t s_end = min(P, (kb + kc) * 32);
-        for (uint32_t s = kb * 32 + warp; s < s_end; s += nwarp) {
-          const uint32_t cc = (s >> 5) - kb, j = s & 31;
-          const uint32_t x = vs[lane * PITCH + cc];
-          uint32_t val = DIST_MAX;
-          bool write = v < p.V;
-          if ((x >> j) & 1u) {
-            if (use_ovf && ((os[lane * PITCH + cc] >> j) & 1u)) {
-              write = false;  // written directly by the level kernel
-            } else {
+      if (!reach && warp < kc) {
+        const uint32_t cc = warp;
+        const uint32_t vl = v0 + 4 * lane;  // this lane's first vertex
+        const uint4 x = *reinterpret_cast<const uint4*>(vs + cc * MAT_TV + 4 * lane);
+        const uint4 o = *reinterpret_cast<const uint4*>(os + cc * MAT_TV + 4 * lane);
+        uint4 pl[MAT_NPMAX];
+#pragma unroll
+        for (int b = 0; b < MAT_NPMAX; ++b)
+          pl[b] = (b < (int)npu)
+                      ? *reinterpret_cast<const uint4*>(ps + (b * KC + cc) * MAT_TV + 4 * lane)
+                      : make_uint4(0, 0, 0, 0);
+        const uint32_t s0 = (kb + cc) * 32;
+        const uint32_t jn = min(32u, P - s0);
+        for (uint32_t j = 0; j < jn; ++j) {
+          uint32_t dv[4];
+          const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+          const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
+          bool skip = false;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            uint32_t val = DIST_MAX;
+            if ((xs[t] >> j) & 1u) {
               val = 0;
-              for (uint32_t b = 0; b < npu; ++b)
-                val |= ((ps[(b * 32 + lane) * PITCH + cc] >> j) & 1u) << b;
+#pragma unroll
+              for (int b = 0; b < MAT_NPMAX; ++b) {
+                const uint32_t w = t == 0 ? pl[b].x : t == 1 ? pl[b].y : t == 2 ? pl[b].z : pl[b].w;
+                val |= ((w >> j) & 1u) << b;
+              }
+              if ((ov[t] >> j) & 1u) skip = true;  // written by the level kernel
             }
+            dv[t] = val;
           }
-          if (write) dist[(size_t)s * p.V + v] = val;
+          uint32_t* row = dist + (size_t)(s0 + j) * p.V + vl;
+          if (vec_ok && !skip && vl + 3 < p.V) {
+            *reinterpret_cast<uint4*>(row) = make_uint4(dv[0], dv[1], dv[2], dv[3]);
+          } else {
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+              if (vl + t < p.V && !((ov[t] >> j) & 1u && (xs[t] >> j) & 1u)) row[t] = dv[t];
+          }
         }
       }
       __syncthreads();
@@ -762,8 +937,8 @@ static void fill_info(int num_sms, LevelKernelInfo* k) {
   k->level_grid = num_sms * occ;
   k->mat_block = MAT_BLOCK;
   constexpr int KC = W < MAT_KC ? W : MAT_KC;
-  // vis + ovf + up to 32 planes, each [32][KC+1] u32
-  k->mat_smem = (size_t)(2 + 32) * 32 * (KC + 1) * sizeof(uint32_t);
+  // vis + ovf + up to MAT_NPMAX planes, each [KC][MAT_TV] u32
+  k->mat_smem = (size_t)(2 + MAT_NPMAX) * KC * MAT_TV * sizeof(uint32_t);
   cudaFuncSetAttribute(materialize_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)k->mat_smem);
   int mocc = 0;
