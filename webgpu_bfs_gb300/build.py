@@ -47,13 +47,15 @@ def _stale(src: Path, obj: Path, newest_header: float) -> bool:
     return src.stat().st_mtime > t or newest_header > t
 
 
-def _compile(src: Path, obj: Path, verbose: bool) -> None:
+def _compile(src: Path, obj: Path, verbose: bool, defines=()) -> None:
+    dflags = [f"-D{d}" for d in defines]
     if src.suffix == ".cu":
-        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *dflags, "-c", str(src), "-o", str(obj)]
         if os.environ.get("MSBFS_PTXAS_VERBOSE"):
             cmd += ["-Xptxas", "-v"]
     else:
-        cmd = ["g++", *CXX_FLAGS, f"-I{_cuda_include()}", "-c", str(src), "-o", str(obj)]
+        cmd = ["g++", *CXX_FLAGS, *dflags, f"-I{_cuda_include()}", "-c", str(src), "-o",
+               str(obj)]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -63,11 +65,18 @@ def _compile(src: Path, obj: Path, verbose: bool) -> None:
         print(r.stderr, file=sys.stderr)
 
 
-def build_native(verbose: bool = False, force: bool = False) -> Path:
-    """Builds (if needed) and returns the path of libmsbfs.so."""
-    OBJDIR.mkdir(parents=True, exist_ok=True)
+def build_native(verbose: bool = False, force: bool = False, defines=(),
+                 out_dir: Path | None = None) -> Path:
+    """Builds (if needed) and returns the path of libmsbfs.so.
+
+    `defines` are tuning macros (e.g. MSBFS_PULL_CH=8) and `out_dir` an
+    alternative output folder, for building tuning variants side by side."""
+    libdir = Path(out_dir) if out_dir else LIBDIR
+    objdir = libdir / "obj"
+    lib = libdir / "libmsbfs.so"
+    objdir.mkdir(parents=True, exist_ok=True)
     # Objects built on another host architecture are never reused.
-    stamp = LIBDIR / "arch.txt"
+    stamp = libdir / "arch.txt"
     arch = platform.machine()
     if not stamp.exists() or stamp.read_text().strip() != arch:
         force = True
@@ -76,18 +85,18 @@ def build_native(verbose: bool = False, force: bool = False) -> Path:
     jobs = []
     objs = []
     for src in sources:
-        obj = OBJDIR / (src.name + ".o")
+        obj = objdir / (src.name + ".o")
         objs.append(obj)
         if force or _stale(src, obj, newest_header):
             jobs.append((src, obj))
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
-            futs = [ex.submit(_compile, s, o, verbose) for s, o in jobs]
+            futs = [ex.submit(_compile, s, o, verbose, defines) for s, o in jobs]
             for f in futs:
                 f.result()
-    lib_time = LIB.stat().st_mtime if LIB.exists() else 0.0
+    lib_time = lib.stat().st_mtime if lib.exists() else 0.0
     if force or jobs or any(o.stat().st_mtime > lib_time for o in objs):
-        tmp = LIB.with_suffix(".so.tmp")
+        tmp = lib.with_suffix(".so.tmp")
         cmd = [_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs),
                "-lpthread", "-Xlinker", "-z,defs"]
         if verbose:
@@ -95,9 +104,9 @@ def build_native(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
     stamp.write_text(arch + "\n")
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -124,6 +124,8 @@ struct LevelParams {
   uint32_t* hcand;    // [n_heavy][W] candidate words of sliced vertices
   uint32_t* hcount;   // [n_heavy] slices finished this level
   uint32_t bits_div;  // bitmap check when the frontier holds < V / bits_div vertices
+  uint32_t n_order;
+  const uint32_t* order;  // vertices with 0 < in-degree <= split, in-degree descending
 };
 
 // Launch helpers implemented in level_kernels.cu / cta_kernel.cu.

@@ -52,6 +52,10 @@ struct msbfs_graph {
   uint32_t n_heavy = 0;
   uint32_t n_hchunks = 0;
   HeavyChunk* hchunks = nullptr;
+  // Bottom-up work order: vertices with 0 < in-degree <= split, in-degree
+  // descending, ids ascending within a degree.
+  uint32_t n_order = 0;
+  uint32_t* order = nullptr;
 };
 
 namespace {
@@ -314,6 +318,8 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   p.split = g->split;
   p.n_hchunks = g->n_hchunks;
   p.hchunks = g->hchunks;
+  p.n_order = g->n_order;
+  p.order = g->order;
   int rc;
   void* ptr;
   if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4))) return rc;
@@ -706,6 +712,31 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
   if (!chunks.empty())
     CK(cudaMemcpy(g->hchunks, chunks.data(), chunks.size() * sizeof(HeavyChunk),
                   cudaMemcpyHostToDevice));
+  // Bottom-up work list: the vertices with 0 < in-degree <= split. Ascending
+  // ids by default (neighbouring vertices share cache lines of the visited and
+  // frontier rows); MSBFS_ORDER_BY_ID=0 sorts by in-degree, descending, which
+  // measured ~7% slower on R-MAT scale 22.
+  {
+#ifndef MSBFS_ORDER_BY_ID
+#define MSBFS_ORDER_BY_ID 1
+#endif
+    auto key = [&](uint32_t d) { return MSBFS_ORDER_BY_ID ? 0u : g->split - d; };
+    std::vector<uint32_t> start(g->split + 2, 0);
+    for (size_t v = 0; v < V; ++v) {
+      const uint32_t d = t.off[v + 1] - t.off[v];
+      if (d > 0 && d <= g->split) start[key(d) + 1]++;
+    }
+    for (uint32_t i = 1; i < start.size(); ++i) start[i] += start[i - 1];
+    std::vector<uint32_t> order(start.back());
+    for (size_t v = 0; v < V; ++v) {
+      const uint32_t d = t.off[v + 1] - t.off[v];
+      if (d > 0 && d <= g->split) order[start[key(d)]++] = (uint32_t)v;
+    }
+    g->n_order = (uint32_t)order.size();
+    CK(cudaMalloc((void**)&g->order, std::max<size_t>(order.size(), 1) * 4));
+    if (!order.empty())
+      CK(cudaMemcpy(g->order, order.data(), order.size() * 4, cudaMemcpyHostToDevice));
+  }
   *out = g.release();
   return MSBFS_OK;
 }
@@ -730,6 +761,7 @@ void free_graph(msbfs_graph* g) {
   cudaFree(g->off);
   cudaFree(g->idx);
   cudaFree(g->hchunks);
+  cudaFree(g->order);
   delete g;
 }
 

@@ -30,7 +30,15 @@ namespace msbfs {
 
 constexpr int LEVEL_BLOCK = 256;
 constexpr int BQ_CAP = 2048;  // discovered vertices staged per block
-constexpr int CH = 4;         // in-neighbours gathered per chunk
+#ifndef MSBFS_PULL_CH
+#define MSBFS_PULL_CH 4
+#endif
+#ifndef MSBFS_LEVEL_MIN_BLOCKS
+// 6 resident blocks of 256 threads (48 warps per SM): the bottom-up gathers
+// are latency-bound, and the extra warps outweigh the few spilled registers.
+#define MSBFS_LEVEL_MIN_BLOCKS 6
+#endif
+constexpr int CH = MSBFS_PULL_CH;  // in-neighbours gathered per chunk
 constexpr int MAT_KC = 8;     // words per materialise chunk
 constexpr int MAT_BLOCK = 256;
 constexpr uint32_t FULL = 0xffffffffu;
@@ -411,11 +419,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     }
   }
 
-  // ---- (2) all other vertices
-  // Tiles are claimed dynamically: on power-law graphs the expensive vertices
-  // cluster (R-MAT puts its hubs at low ids), so a static split leaves most
-  // warps idle behind a few.
-  const uint32_t ntiles = (p.V + GPW - 1) / GPW;
+  // ---- (2) all other vertices with in-edges, in the graph's work order
+  // (in-degree descending, ids ascending within a degree), so the groups of a
+  // warp walk in-edge lists of equal length and vertices without in-edges
+  // cost nothing. Tiles are claimed dynamically: the expensive vertices come
+  // first and a static split would leave most warps idle behind a few.
+  const uint32_t ntiles = (p.n_order + GPW - 1) / GPW;
   uint32_t tile = 0, tile_end = 0;
   for (;;) {
     if (tile == tile_end) {
@@ -425,13 +434,13 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
       if (tile >= ntiles) break;
       tile_end = min(tile + TILE_BATCH, ntiles);
     }
-    const uint32_t v = tile * GPW + gid;
+    const uint32_t oi = tile * GPW + gid;
     ++tile;
-    uint32_t beg = 0, end = 0;
-    if (v < p.V) {
+    uint32_t v = 0, beg = 0, end = 0;
+    if (oi < p.n_order) {
+      v = __ldg(p.order + oi);
       beg = __ldg(in_off + v);
       end = __ldg(in_off + v + 1);
-      if (end - beg > p.split) end = beg;  // sliced: handled in part (1)
     }
     Words<VEC> needed, visw, cand;
 #pragma unroll
@@ -446,15 +455,28 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     if (lig == 0 && need) cnt.active += 1;
 
     if (need && !heavy) {
+      // The next chunk's in-neighbour ids are fetched while the current
+      // chunk's frontier rows are in flight.
+      constexpr int NI = LPV >= CH ? 1 : CH;  // ids held per lane
+      uint32_t ids[NI];
+#pragma unroll
+      for (int j = 0; j < NI; ++j) {
+        const uint32_t e = beg + (LPV >= CH ? lig : j);
+        ids[j] = ((LPV < CH || lig < CH) && e < end) ? __ldg(in_idx + e) : FULL;
+      }
       for (uint32_t e0 = beg; e0 < end; e0 += CH) {
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
-          const uint32_t mine = (lig < CH && e0 + lig < end) ? __ldg(in_idx + e0 + lig) : FULL;
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(gmask, mine, gbase + j);
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(gmask, ids[0], gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = (e0 + j < end) ? __ldg(in_idx + e0 + j) : FULL;
+          for (int j = 0; j < CH; ++j) u[j] = ids[j];
+        }
+#pragma unroll
+        for (int j = 0; j < NI; ++j) {
+          const uint32_t e = e0 + CH + (LPV >= CH ? lig : j);
+          ids[j] = ((LPV < CH || lig < CH) && e < end) ? __ldg(in_idx + e) : FULL;
         }
         Words<VEC> f[CH];
         if (lig == 0) cnt.edges += min((uint32_t)CH, end - e0);
@@ -677,7 +699,7 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
 }
 
 template <int W>
-__global__ void __launch_bounds__(LEVEL_BLOCK)
+__global__ void __launch_bounds__(LEVEL_BLOCK, MSBFS_LEVEL_MIN_BLOCKS)
     level_kernel(LevelParams p, cudaGraphConditionalHandle h) {
   __shared__ BlockQueue bq;
   __shared__ unsigned long long s_red[5][LEVEL_BLOCK / 32];
@@ -794,8 +816,114 @@ __device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __c
 constexpr int MAT_TV = 128;
 constexpr int MAT_NPMAX = 8;
 
+// Store phase of one warp: word cc of the tile, 4 vertices per lane, rows
+// s0 .. s0+jn-1. NPU (planes in use) is a template argument so the plane
+// words stay in registers without a spill-prone runtime-sized array.
+template <int NPU, int KC>
+__device__ __forceinline__ void mat_store_rows(const uint32_t* vs, const uint32_t* os,
+                                               const uint32_t* ps, uint32_t cc, uint32_t lane,
+                                               uint32_t* dist, uint32_t V, uint32_t v0,
+                                               uint32_t s0, uint32_t jn, bool vec_ok) {
+  const uint32_t vl = v0 + 4 * lane;
+  const uint4 x = *reinterpret_cast<const uint4*>(vs + cc * MAT_TV + 4 * lane);
+  const uint4 o = *reinterpret_cast<const uint4*>(os + cc * MAT_TV + 4 * lane);
+  uint4 pl[NPU > 0 ? NPU : 1];
+#pragma unroll
+  for (int b = 0; b < NPU; ++b)
+    pl[b] = *reinterpret_cast<const uint4*>(ps + (b * KC + cc) * MAT_TV + 4 * lane);
+  const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+  const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
+  const bool any_ovf = (o.x | o.y | o.z | o.w) != 0;
+  const bool full = vec_ok && vl + 3 < V;
+  for (uint32_t j = 0; j < jn; ++j) {
+    uint32_t dv[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      uint32_t val = 0;
+#pragma unroll
+      for (int b = 0; b < NPU; ++b) {
+        const uint32_t w = t == 0 ? pl[b].x : t == 1 ? pl[b].y : t == 2 ? pl[b].z : pl[b].w;
+        val |= ((w >> j) & 1u) << b;
+      }
+      dv[t] = ((xs[t] >> j) & 1u) ? val : DIST_MAX;
+    }
+    uint32_t* row = dist + (size_t)(s0 + j) * V + vl;
+    bool skip = false;
+    if (any_ovf) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) skip |= ((ov[t] & xs[t]) >> j) & 1u;
+    }
+    if (full && !skip) {
+      *reinterpret_cast<uint4*>(row) = make_uint4(dv[0], dv[1], dv[2], dv[3]);
+    } else {
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (vl + t < V && !(((ov[t] & xs[t]) >> j) & 1u)) row[t] = dv[t];
+    }
+  }
+}
+
+template <int KC>
+__device__ __forceinline__ void mat_store_dispatch(uint32_t npu, const uint32_t* vs,
+                                                   const uint32_t* os, const uint32_t* ps,
+                                                   uint32_t cc, uint32_t lane, uint32_t* dist,
+                                                   uint32_t V, uint32_t v0, uint32_t s0,
+                                                   uint32_t jn, bool vec_ok) {
+  switch (npu) {
+#define MAT_CASE(n) \
+  case n: mat_store_rows<n, KC>(vs, os, ps, cc, lane, dist, V, v0, s0, jn, vec_ok); break;
+    MAT_CASE(0) MAT_CASE(1) MAT_CASE(2) MAT_CASE(3) MAT_CASE(4)
+    MAT_CASE(5) MAT_CASE(6) MAT_CASE(7) MAT_CASE(8)
+#undef MAT_CASE
+    default: break;
+  }
+}
+
+// Loads (and zeroes) words [kb, kb+KC) of the tile's vertices from one
+// vertex-major array into word-major shared memory.
+template <int W, int KC>
+__device__ __forceinline__ void mat_stage(uint32_t* arr, uint32_t* dst, uint32_t V, uint32_t v0,
+                                          uint32_t kb) {
+  if constexpr (KC % 4 == 0) {
+    constexpr int Q = KC / 4;  // 16-byte pieces per vertex row chunk
+    for (uint32_t i = threadIdx.x; i < MAT_TV * Q; i += blockDim.x) {
+      const uint32_t r = i / Q, q = i % Q, v = v0 + r;
+      uint4 x = make_uint4(0, 0, 0, 0);
+      if (v < V) {
+        uint4* a = reinterpret_cast<uint4*>(arr + (size_t)v * W + kb + 4 * q);
+        x = *a;
+        *a = make_uint4(0, 0, 0, 0);
+      }
+      dst[(4 * q + 0) * MAT_TV + r] = x.x;
+      dst[(4 * q + 1) * MAT_TV + r] = x.y;
+      dst[(4 * q + 2) * MAT_TV + r] = x.z;
+      dst[(4 * q + 3) * MAT_TV + r] = x.w;
+    }
+  } else {
+    for (uint32_t i = threadIdx.x; i < MAT_TV * KC; i += blockDim.x) {
+      const uint32_t r = i / KC, cc = i % KC, v = v0 + r;
+      uint32_t x = 0;
+      if (v < V) {
+        uint32_t* a = arr + (size_t)v * W + kb + cc;
+        x = *a;
+        *a = 0;
+      }
+      dst[cc * MAT_TV + r] = x;
+    }
+  }
+}
+
+// Turns visited words + level planes into the source-major u32 distance rows
+// (or copies the visited words out as a reachability bitmask), and zeroes the
+// words it read so the next pass starts from clean buffers. A block stages a
+// tile of MAT_TV consecutive vertices x KC words in shared memory (word-major,
+// so a lane reads its 4 vertices with one 16-byte load); warp c then owns word
+// c: it keeps the tile's visited/plane words of its 4 vertices in registers
+// and writes the 32 rows s = 32*(kb+c) + j as 512-byte contiguous segments
+// (one 16-byte store per lane per row). Words past the pass's last source
+// are zero in every array, so whole KC-word chunks are staged.
 template <int W>
-__global__ void __launch_bounds__(MAT_BLOCK) materialize_kernel(LevelParams p) {
+__global__ void __launch_bounds__(MAT_BLOCK, 4) materialize_kernel(LevelParams p) {
   extern __shared__ __align__(16) uint32_t sm[];
   constexpr int KC = W < MAT_KC ? W : MAT_KC;
   const PassDesc* dsc = p.desc;
@@ -818,70 +946,25 @@ __global__ void __launch_bounds__(MAT_BLOCK) materialize_kernel(LevelParams p) {
     const uint32_t v0 = tile * MAT_TV;
     for (uint32_t kb = 0; kb < Wu; kb += KC) {
       const uint32_t kc = min((uint32_t)KC, Wu - kb);
-      for (uint32_t i = threadIdx.x; i < MAT_TV * kc; i += blockDim.x) {
-        const uint32_t r = i / kc, cc = i % kc, v = v0 + r;
-        uint32_t x = 0, o = 0;
-        if (v < p.V) {
-          const size_t a = (size_t)v * W + kb + cc;
-          x = p.vis[a];
-          p.vis[a] = 0;
-          if (use_ovf) {
-            o = p.ovf[a];
-            p.ovf[a] = 0;
-          }
-          for (uint32_t b = 0; b < npu; ++b) {
-            ps[(b * KC + cc) * MAT_TV + r] = p.planes[b * VW + a];
-            p.planes[b * VW + a] = 0;
-          }
-          if (reach) reach[(size_t)v * dsc->reach_wpv + dsc->reach_col + kb + cc] = x;
-        } else {
-          for (uint32_t b = 0; b < npu; ++b) ps[(b * KC + cc) * MAT_TV + r] = 0;
-        }
-        vs[cc * MAT_TV + r] = x;
-        os[cc * MAT_TV + r] = o;
+      mat_stage<W, KC>(p.vis, vs, p.V, v0, kb);
+      if (use_ovf) {
+        mat_stage<W, KC>(p.ovf, os, p.V, v0, kb);
+      } else {
+        for (uint32_t i = threadIdx.x; i < KC * MAT_TV; i += blockDim.x) os[i] = 0;
       }
+      for (uint32_t b = 0; b < npu; ++b)
+        mat_stage<W, KC>(p.planes + b * VW, ps + b * KC * MAT_TV, p.V, v0, kb);
       __syncthreads();
-      if (!reach && warp < kc) {
-        const uint32_t cc = warp;
-        const uint32_t vl = v0 + 4 * lane;  // this lane's first vertex
-        const uint4 x = *reinterpret_cast<const uint4*>(vs + cc * MAT_TV + 4 * lane);
-        const uint4 o = *reinterpret_cast<const uint4*>(os + cc * MAT_TV + 4 * lane);
-        uint4 pl[MAT_NPMAX];
-#pragma unroll
-        for (int b = 0; b < MAT_NPMAX; ++b)
-          pl[b] = (b < (int)npu)
-                      ? *reinterpret_cast<const uint4*>(ps + (b * KC + cc) * MAT_TV + 4 * lane)
-                      : make_uint4(0, 0, 0, 0);
-        const uint32_t s0 = (kb + cc) * 32;
-        const uint32_t jn = min(32u, P - s0);
-        for (uint32_t j = 0; j < jn; ++j) {
-          uint32_t dv[4];
-          const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
-          const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
-          bool skip = false;
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            uint32_t val = DIST_MAX;
-            if ((xs[t] >> j) & 1u) {
-              val = 0;
-#pragma unroll
-              for (int b = 0; b < MAT_NPMAX; ++b) {
-                const uint32_t w = t == 0 ? pl[b].x : t == 1 ? pl[b].y : t == 2 ? pl[b].z : pl[b].w;
-                val |= ((w >> j) & 1u) << b;
-              }
-              if ((ov[t] >> j) & 1u) skip = true;  // written by the level kernel
-            }
-            dv[t] = val;
-          }
-          uint32_t* row = dist + (size_t)(s0 + j) * p.V + vl;
-          if (vec_ok && !skip && vl + 3 < p.V) {
-            *reinterpret_cast<uint4*>(row) = make_uint4(dv[0], dv[1], dv[2], dv[3]);
-          } else {
-#pragma unroll
-            for (int t = 0; t < 4; ++t)
-              if (vl + t < p.V && !((ov[t] >> j) & 1u && (xs[t] >> j) & 1u)) row[t] = dv[t];
-          }
+      if (reach) {
+        for (uint32_t i = threadIdx.x; i < MAT_TV * kc; i += blockDim.x) {
+          const uint32_t r = i / kc, cc = i % kc, v = v0 + r;
+          if (v < p.V)
+            reach[(size_t)v * dsc->reach_wpv + dsc->reach_col + kb + cc] = vs[cc * MAT_TV + r];
         }
+      } else if (warp < kc) {
+        const uint32_t s0 = (kb + warp) * 32;
+        mat_store_dispatch<KC>(npu, vs, os, ps, warp, lane, dist, p.V, v0, s0,
+                               min(32u, P - s0), vec_ok);
       }
       __syncthreads();
     }
@@ -939,6 +1022,7 @@ static void fill_info(int num_sms, LevelKernelInfo* k) {
   constexpr int KC = W < MAT_KC ? W : MAT_KC;
   // vis + ovf + up to MAT_NPMAX planes, each [KC][MAT_TV] u32
   k->mat_smem = (size_t)(2 + MAT_NPMAX) * KC * MAT_TV * sizeof(uint32_t);
+  static_assert(MAT_KC % 4 == 0 && MAT_TV == 4 * 32, "tile shape");
   cudaFuncSetAttribute(materialize_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)k->mat_smem);
   int mocc = 0;
