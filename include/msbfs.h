@@ -45,6 +45,8 @@ extern "C" {
 #define MSBFS_ERR_INVALID_GRAPH 6
 #define MSBFS_ERR_INVALID_ARGUMENT 7
 #define MSBFS_ERR_NO_DEVICE 8
+/* The graph does not fit the fixed scratch of msbfs_run_cta_noalloc. */
+#define MSBFS_ERR_SCRATCH_TOO_SMALL 9
 
 /* ---- methods: same names and order as GpuBfsMethod (engine.rs:33-53) ------
  * Every method produces identical bytes. On GB300 they map onto four kernel
@@ -223,6 +225,43 @@ int msbfs_run_reachability(msbfs_engine *engine, const msbfs_graph *graph,
 int msbfs_traversed_edges_device(msbfs_engine *engine, const msbfs_graph *graph,
                                  const uint32_t *dist_device,
                                  size_t num_sources, uint64_t *out_edges);
+
+/* ------------------------------------------------------------------------
+ * Multi-source BFS that allocates nothing. No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: code that runs while a CUDA stream
+ * capture is active on the device (the allocator may not be used then), hosts
+ * that hand all device memory to their own pool and forbid allocations from
+ * libraries, and long-running services that reserve their memory up front.
+ * Every other entry point allocates engine-owned device buffers; this one
+ * uses no engine. It runs the one-block-per-source BFS (the kernel behind
+ * MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS) with its scratch -- a copy of the
+ * sources, the source cursor and one frontier queue of 2*V u32 per resident
+ * block -- in a fixed device array of MSBFS_NOALLOC_SCRATCH_BYTES inside the
+ * library. Every GPU that loads the library holds that array until exit.
+ *
+ * Inputs and outputs stay the caller's: the CSR arrays and the S*V u32
+ * distance matrix are DEVICE pointers (dist[s*V + v], unreachable =
+ * 0xFFFFFFFF, the same bytes as msbfs_run_ms_bfs); `sources` is a HOST array,
+ * validated like msbfs_run_ms_bfs (MSBFS_ERR_SOURCE_OOB) and copied into the
+ * fixed array. Work is queued on `cuda_stream` (NULL = legacy default stream)
+ * and the call returns without waiting. Graphs with more than
+ * MSBFS_NOALLOC_MAX_VERTICES vertices are rejected with
+ * MSBFS_ERR_SCRATCH_TOO_SMALL before anything is queued.
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture begins. All calls share the one array, which keeps the last call's
+ * contents (the cursor is cleared by each call): calls that overlap on the
+ * GPU -- on different streams, or before the previous call's work finished
+ * on another stream -- race on it and must be serialised by the caller. */
+#define MSBFS_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define MSBFS_NOALLOC_MAX_VERTICES 1048576u
+int msbfs_run_cta_noalloc(int device, size_t num_vertices,
+                          const uint32_t *row_offsets_device,
+                          const uint32_t *col_indices_device,
+                          const uint32_t *sources, size_t num_sources,
+                          uint32_t *dist_device, void *cuda_stream);
 
 /* ===================== graph core (crates/core) =========================== */
 

@@ -96,6 +96,8 @@ SIGNATURES = {
                                          C.POINTER(Stats)]),
     "msbfs_traversed_edges_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
                                                u64p]),
+    "msbfs_run_cta_noalloc": (C.c_int, [C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, u32p,
+                                        C.c_size_t, C.c_void_p, C.c_void_p]),
     "msbfs_csr_free": (None, [C.POINTER(Csr)]),
     "msbfs_csr_from_edge_list": (C.c_int, [C.c_size_t, C.c_size_t, u32p, u32p,
                                            C.POINTER(Csr)]),

@@ -11,6 +11,10 @@
 // fallback), distances are exact u32 written into the caller's row, and the
 // grid is persistent: each resident block pulls the next source from an
 // atomic cursor until all sources are done. No block ever waits on another.
+#include <algorithm>
+#include <mutex>
+
+#include "../../include/msbfs.h"
 #include "device_common.cuh"
 
 namespace msbfs {
@@ -112,4 +116,93 @@ void launch_cta(const CtaParams& p, int grid, int block, size_t smem, cudaStream
   cta_bfs_kernel<<<grid, block, smem, s>>>(p);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free form of the CTA-per-source launch.
+//
+// Its scratch -- a copy of the sources, the source cursor and one frontier
+// queue slab (2*V words) per resident block -- lives in this fixed array
+// instead of engine-owned cudaMalloc memory, so the entry point below never
+// allocates. Every GPU that loads the library holds the array until exit.
+// Layout in u32 words: [0] source cursor, [NOALLOC_SRC_OFF, +NOALLOC_SRC_CAP)
+// sources of the current chunk, [NOALLOC_Q_OFF, end) queue slabs.
+constexpr size_t NOALLOC_WORDS = MSBFS_NOALLOC_SCRATCH_BYTES / sizeof(uint32_t);
+constexpr size_t NOALLOC_SRC_OFF = 64;
+constexpr size_t NOALLOC_SRC_CAP = 65536;
+constexpr size_t NOALLOC_Q_OFF = NOALLOC_SRC_OFF + NOALLOC_SRC_CAP;
+static __device__ __align__(256) uint32_t g_noalloc_scratch[NOALLOC_WORDS];
+
+namespace {
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_addr[64];  // device address of the array, per device
+}  // namespace
+
 }  // namespace msbfs
+
+extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
+                                     const uint32_t* row_offsets_device,
+                                     const uint32_t* col_indices_device,
+                                     const uint32_t* sources, size_t num_sources,
+                                     uint32_t* dist_device, void* cuda_stream) {
+  using namespace msbfs;
+  if (num_sources == 0) return MSBFS_OK;
+  if (device < 0 || device >= 64) return MSBFS_ERR_NO_DEVICE;
+  if (!row_offsets_device || !col_indices_device || !sources || !dist_device)
+    return MSBFS_ERR_INVALID_ARGUMENT;
+  if (num_vertices == 0) return MSBFS_ERR_EMPTY_GRAPH;
+  for (size_t i = 0; i < num_sources; ++i)
+    if ((size_t)sources[i] >= num_vertices) return MSBFS_ERR_SOURCE_OOB;
+  // Size limits, checked before touching the device: the visited bitmap must
+  // fit shared memory and at least one queue slab must fit the scratch array.
+  if (num_vertices > MSBFS_NOALLOC_MAX_VERTICES ||
+      NOALLOC_Q_OFF + 2 * num_vertices > NOALLOC_WORDS)
+    return MSBFS_ERR_SCRATCH_TOO_SMALL;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return MSBFS_ERR_NO_DEVICE;
+  }
+  // Once per device, with that device current: the array's device address
+  // (in host code the symbol itself is only a host-side stand-in).
+  uint32_t* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return MSBFS_ERR_CUDA;
+      }
+      g_noalloc_addr[device] = static_cast<uint32_t*>(p);
+    }
+    base = g_noalloc_addr[device];
+  }
+  const uint32_t V = (uint32_t)num_vertices;
+  int grid = 0, block = 0;
+  size_t smem = 0;
+  if (!cta_launch_shape(V, device, &grid, &block, &smem)) return MSBFS_ERR_SCRATCH_TOO_SMALL;
+  const size_t slabs = (NOALLOC_WORDS - NOALLOC_Q_OFF) / (2 * (size_t)V);
+  const cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  for (size_t s0 = 0; s0 < num_sources; s0 += NOALLOC_SRC_CAP) {
+    const size_t n = std::min(NOALLOC_SRC_CAP, num_sources - s0);
+    // The cursor must start at zero; queue slabs need no clearing.
+    if (cudaMemsetAsync(base, 0, sizeof(uint32_t), s) != cudaSuccess ||
+        cudaMemcpyAsync(base + NOALLOC_SRC_OFF, sources + s0, n * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      cudaGetLastError();
+      return MSBFS_ERR_CUDA;
+    }
+    CtaParams cp{};
+    cp.V = V;
+    cp.off = row_offsets_device;
+    cp.idx = col_indices_device;
+    cp.sources = base + NOALLOC_SRC_OFF;
+    cp.num_sources = (uint32_t)n;
+    cp.dist = dist_device + s0 * num_vertices;
+    cp.gqueue = base + NOALLOC_Q_OFF;
+    cp.work = base;
+    const int blocks = (int)std::min<size_t>({(size_t)grid, n, slabs});
+    launch_cta(cp, blocks, block, smem, s);
+    if (cudaGetLastError() != cudaSuccess) return MSBFS_ERR_CUDA;
+  }
+  return MSBFS_OK;
+}
