@@ -373,7 +373,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
           if (e0 + j < end) {
             const uint32_t u = __ldg(in_idx + e0 + j);
             if (in_frontier(fb, u)) {
-              if (lig == 0) cnt.rows += 1;
+              cnt.rows += 1;
               Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
 #pragma unroll
               for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
@@ -459,6 +459,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
       // chunk's frontier rows are in flight.
       constexpr int NI = LPV >= CH ? 1 : CH;  // ids held per lane
       uint32_t ids[NI];
+      bool lane_sat = !any_bits<VEC>(needed);
 #pragma unroll
       for (int j = 0; j < NI; ++j) {
         const uint32_t e = beg + (LPV >= CH ? lig : j);
@@ -480,10 +481,11 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         }
         Words<VEC> f[CH];
         if (lig == 0) cnt.edges += min((uint32_t)CH, end - e0);
+        // A lane whose own words are covered skips its 16-byte pieces.
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (u[j] != FULL && in_frontier(fb, u[j])) {
-            if (lig == 0) cnt.rows += 1;
+          if (!lane_sat && u[j] != FULL && in_frontier(fb, u[j])) {
+            cnt.rows += 1;
             f[j] = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
           } else {
 #pragma unroll
@@ -499,6 +501,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
           cand.w[q] = c;
           sat &= (c & needed.w[q]) == needed.w[q];
         }
+        lane_sat = sat;
         if (__ballot_sync(gmask, !sat) == 0) break;
       }
     }
@@ -523,7 +526,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
           if (e0 + j < hend) {
             const uint32_t u = __ldg(in_idx + e0 + j);
             if (in_frontier(fb, u)) {
-              if (lig == 0) cnt.rows += 1;
+              cnt.rows += 1;
               Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
 #pragma unroll
               for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
@@ -641,7 +644,7 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
     r.edges = c->c_edges;
     r.new_vertices = c->c_newv;
     r.new_pairs = c->c_pairs;
-    r.rows = c->c_rows;
+    r.rows = c->c_rows / (p.W >= 4 ? p.W / 4 : 1);  // counted per 16-byte piece
     r.t_start = c->t_start;
     r.t_end = globaltimer();
     p.log[L] = r;
@@ -813,27 +816,64 @@ __device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __c
 // c: it keeps the tile's visited/plane words of its 4 vertices in registers
 // and writes the 32 rows s = 32*(kb+c) + j as 512-byte contiguous segments
 // (one 16-byte store per lane per row).
-constexpr int MAT_TV = 128;
+constexpr int MAT_TV = 128;  // vertices per work item (4 per lane)
 constexpr int MAT_NPMAX = 8;
 
-// Store phase of one warp: word cc of the tile, 4 vertices per lane, rows
-// s0 .. s0+jn-1. NPU (planes in use) is a template argument so the plane
-// words stay in registers without a spill-prone runtime-sized array.
-template <int NPU, int KC>
-__device__ __forceinline__ void mat_store_rows(const uint32_t* vs, const uint32_t* os,
-                                               const uint32_t* ps, uint32_t cc, uint32_t lane,
-                                               uint32_t* dist, uint32_t V, uint32_t v0,
-                                               uint32_t s0, uint32_t jn, bool vec_ok) {
+// One work item: word c of the 128 vertices v0 .. v0+127, i.e. the 32 sources
+// 32c .. 32c+31 of this pass. Lane l owns vertices v0+4l .. v0+4l+3: it loads
+// their visited / overflow / plane words (strided by W words; the warps of a
+// block take consecutive words of the same vertices, so the 32-byte sectors
+// are shared through L1), zeroes them, and writes the 32 distance rows as
+// 512-byte contiguous segments (one 16-byte store per lane per row). NPU
+// (planes in use) is a template argument so the plane words stay in
+// registers.
+template <int NPU>
+__device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint32_t c,
+                                         uint32_t lane, uint32_t P, bool use_ovf,
+                                         bool vec_ok) {
+  const uint32_t W = p.W;
+  const uint32_t V = p.V;
+  const size_t VW = (size_t)V * W;
   const uint32_t vl = v0 + 4 * lane;
-  const uint4 x = *reinterpret_cast<const uint4*>(vs + cc * MAT_TV + 4 * lane);
-  const uint4 o = *reinterpret_cast<const uint4*>(os + cc * MAT_TV + 4 * lane);
-  uint4 pl[NPU > 0 ? NPU : 1];
+  uint32_t xs[4] = {0, 0, 0, 0}, ov[4] = {0, 0, 0, 0};
+  uint32_t pl[NPU > 0 ? NPU : 1][4];
 #pragma unroll
   for (int b = 0; b < NPU; ++b)
-    pl[b] = *reinterpret_cast<const uint4*>(ps + (b * KC + cc) * MAT_TV + 4 * lane);
-  const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
-  const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
-  const bool any_ovf = (o.x | o.y | o.z | o.w) != 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) pl[b][t] = 0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const uint32_t v = vl + t;
+    if (v < V) {
+      const size_t a = (size_t)v * W + c;
+      xs[t] = p.vis[a];
+      if (use_ovf) ov[t] = p.ovf[a];
+#pragma unroll
+      for (int b = 0; b < NPU; ++b) pl[b][t] = p.planes[b * VW + a];
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const uint32_t v = vl + t;
+    if (v < V) {
+      const size_t a = (size_t)v * W + c;
+      p.vis[a] = 0;
+      if (use_ovf) p.ovf[a] = 0;
+#pragma unroll
+      for (int b = 0; b < NPU; ++b) p.planes[b * VW + a] = 0;
+    }
+  }
+  const PassDesc* dsc = p.desc;
+  if (dsc->reach) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (vl + t < V) dsc->reach[(size_t)(vl + t) * dsc->reach_wpv + dsc->reach_col + c] = xs[t];
+    return;
+  }
+  uint32_t* dist = dsc->dist;
+  const uint32_t s0 = c * 32;
+  const uint32_t jn = min(32u, P - s0);
+  const bool any_ovf = (ov[0] | ov[1] | ov[2] | ov[3]) != 0;
   const bool full = vec_ok && vl + 3 < V;
   for (uint32_t j = 0; j < jn; ++j) {
     uint32_t dv[4];
@@ -841,10 +881,7 @@ __device__ __forceinline__ void mat_store_rows(const uint32_t* vs, const uint32_
     for (int t = 0; t < 4; ++t) {
       uint32_t val = 0;
 #pragma unroll
-      for (int b = 0; b < NPU; ++b) {
-        const uint32_t w = t == 0 ? pl[b].x : t == 1 ? pl[b].y : t == 2 ? pl[b].z : pl[b].w;
-        val |= ((w >> j) & 1u) << b;
-      }
+      for (int b = 0; b < NPU; ++b) val |= ((pl[b][t] >> j) & 1u) << b;
       dv[t] = ((xs[t] >> j) & 1u) ? val : DIST_MAX;
     }
     uint32_t* row = dist + (size_t)(s0 + j) * V + vl;
@@ -863,110 +900,34 @@ __device__ __forceinline__ void mat_store_rows(const uint32_t* vs, const uint32_
   }
 }
 
-template <int KC>
-__device__ __forceinline__ void mat_store_dispatch(uint32_t npu, const uint32_t* vs,
-                                                   const uint32_t* os, const uint32_t* ps,
-                                                   uint32_t cc, uint32_t lane, uint32_t* dist,
-                                                   uint32_t V, uint32_t v0, uint32_t s0,
-                                                   uint32_t jn, bool vec_ok) {
-  switch (npu) {
-#define MAT_CASE(n) \
-  case n: mat_store_rows<n, KC>(vs, os, ps, cc, lane, dist, V, v0, s0, jn, vec_ok); break;
-    MAT_CASE(0) MAT_CASE(1) MAT_CASE(2) MAT_CASE(3) MAT_CASE(4)
-    MAT_CASE(5) MAT_CASE(6) MAT_CASE(7) MAT_CASE(8)
-#undef MAT_CASE
-    default: break;
-  }
-}
-
-// Loads (and zeroes) words [kb, kb+KC) of the tile's vertices from one
-// vertex-major array into word-major shared memory.
-template <int W, int KC>
-__device__ __forceinline__ void mat_stage(uint32_t* arr, uint32_t* dst, uint32_t V, uint32_t v0,
-                                          uint32_t kb) {
-  if constexpr (KC % 4 == 0) {
-    constexpr int Q = KC / 4;  // 16-byte pieces per vertex row chunk
-    for (uint32_t i = threadIdx.x; i < MAT_TV * Q; i += blockDim.x) {
-      const uint32_t r = i / Q, q = i % Q, v = v0 + r;
-      uint4 x = make_uint4(0, 0, 0, 0);
-      if (v < V) {
-        uint4* a = reinterpret_cast<uint4*>(arr + (size_t)v * W + kb + 4 * q);
-        x = *a;
-        *a = make_uint4(0, 0, 0, 0);
-      }
-      dst[(4 * q + 0) * MAT_TV + r] = x.x;
-      dst[(4 * q + 1) * MAT_TV + r] = x.y;
-      dst[(4 * q + 2) * MAT_TV + r] = x.z;
-      dst[(4 * q + 3) * MAT_TV + r] = x.w;
-    }
-  } else {
-    for (uint32_t i = threadIdx.x; i < MAT_TV * KC; i += blockDim.x) {
-      const uint32_t r = i / KC, cc = i % KC, v = v0 + r;
-      uint32_t x = 0;
-      if (v < V) {
-        uint32_t* a = arr + (size_t)v * W + kb + cc;
-        x = *a;
-        *a = 0;
-      }
-      dst[cc * MAT_TV + r] = x;
-    }
-  }
-}
-
 // Turns visited words + level planes into the source-major u32 distance rows
-// (or copies the visited words out as a reachability bitmask), and zeroes the
-// words it read so the next pass starts from clean buffers. A block stages a
-// tile of MAT_TV consecutive vertices x KC words in shared memory (word-major,
-// so a lane reads its 4 vertices with one 16-byte load); warp c then owns word
-// c: it keeps the tile's visited/plane words of its 4 vertices in registers
-// and writes the 32 rows s = 32*(kb+c) + j as 512-byte contiguous segments
-// (one 16-byte store per lane per row). Words past the pass's last source
-// are zero in every array, so whole KC-word chunks are staged.
+// (or copies the visited words out as a reachability bitmask) and zeroes the
+// words it read, so the next pass starts from clean buffers. Warps take
+// (vertex tile, word) items independently: no shared memory, no barriers.
 template <int W>
 __global__ void __launch_bounds__(MAT_BLOCK, 4) materialize_kernel(LevelParams p) {
-  extern __shared__ __align__(16) uint32_t sm[];
-  constexpr int KC = W < MAT_KC ? W : MAT_KC;
   const PassDesc* dsc = p.desc;
   const uint32_t P = dsc->num_sources;
   const uint32_t Wu = (P + 31) / 32;
   const uint32_t dmax = p.ctl->level;
   const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
   const bool use_ovf = dmax >= (1u << p.NP);
-  const size_t VW = (size_t)p.V * W;
-  uint32_t* vs = sm;                  // [KC][MAT_TV]
-  uint32_t* os = vs + KC * MAT_TV;    // [KC][MAT_TV]
-  uint32_t* ps = os + KC * MAT_TV;    // [npu][KC][MAT_TV]
-  uint32_t* dist = dsc->dist;
-  uint32_t* reach = dsc->reach;
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t ntiles = (p.V + MAT_TV - 1) / MAT_TV;
-  const bool vec_ok = (p.V % 4 == 0) && (((uintptr_t)dist & 15) == 0);
-
-  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint32_t v0 = tile * MAT_TV;
-    for (uint32_t kb = 0; kb < Wu; kb += KC) {
-      const uint32_t kc = min((uint32_t)KC, Wu - kb);
-      mat_stage<W, KC>(p.vis, vs, p.V, v0, kb);
-      if (use_ovf) {
-        mat_stage<W, KC>(p.ovf, os, p.V, v0, kb);
-      } else {
-        for (uint32_t i = threadIdx.x; i < KC * MAT_TV; i += blockDim.x) os[i] = 0;
-      }
-      for (uint32_t b = 0; b < npu; ++b)
-        mat_stage<W, KC>(p.planes + b * VW, ps + b * KC * MAT_TV, p.V, v0, kb);
-      __syncthreads();
-      if (reach) {
-        for (uint32_t i = threadIdx.x; i < MAT_TV * kc; i += blockDim.x) {
-          const uint32_t r = i / kc, cc = i % kc, v = v0 + r;
-          if (v < p.V)
-            reach[(size_t)v * dsc->reach_wpv + dsc->reach_col + kb + cc] = vs[cc * MAT_TV + r];
-        }
-      } else if (warp < kc) {
-        const uint32_t s0 = (kb + warp) * 32;
-        mat_store_dispatch<KC>(npu, vs, os, ps, warp, lane, dist, p.V, v0, s0,
-                               min(32u, P - s0), vec_ok);
-      }
-      __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const bool vec_ok = (p.V % 4 == 0) && (((uintptr_t)dsc->dist & 15) == 0);
+  const size_t ntiles = (p.V + MAT_TV - 1) / MAT_TV;
+  const size_t nitems = ntiles * Wu;
+  const size_t warp_g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t it = warp_g; it < nitems; it += nwarps) {
+    const uint32_t v0 = (uint32_t)(it / Wu) * MAT_TV;
+    const uint32_t c = (uint32_t)(it % Wu);
+    switch (npu) {
+#define MAT_CASE(n) \
+  case n: mat_item<n>(p, v0, c, lane, P, use_ovf, vec_ok); break;
+      MAT_CASE(0) MAT_CASE(1) MAT_CASE(2) MAT_CASE(3) MAT_CASE(4)
+      MAT_CASE(5) MAT_CASE(6) MAT_CASE(7) MAT_CASE(8)
+#undef MAT_CASE
+      default: break;
     }
   }
 }
@@ -1019,15 +980,9 @@ static void fill_info(int num_sms, LevelKernelInfo* k) {
   if (occ < 1) occ = 1;
   k->level_grid = num_sms * occ;
   k->mat_block = MAT_BLOCK;
-  constexpr int KC = W < MAT_KC ? W : MAT_KC;
-  // vis + ovf + up to MAT_NPMAX planes, each [KC][MAT_TV] u32
-  k->mat_smem = (size_t)(2 + MAT_NPMAX) * KC * MAT_TV * sizeof(uint32_t);
-  static_assert(MAT_KC % 4 == 0 && MAT_TV == 4 * 32, "tile shape");
-  cudaFuncSetAttribute(materialize_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)k->mat_smem);
+  k->mat_smem = 0;
   int mocc = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mocc, materialize_kernel<W>, MAT_BLOCK,
-                                                k->mat_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mocc, materialize_kernel<W>, MAT_BLOCK, 0);
   if (mocc < 1) mocc = 1;
   k->mat_grid = num_sms * mocc;
 }
