@@ -381,6 +381,28 @@ def run_ours(args, spec):
         dist.destroy_process_group()
 
 
+def run_ncu_case(args, spec):
+    """A single small invocation for ncu captures (few GB on the device)."""
+    os.environ["MSBFS_HOST_LOOP"] = "1"
+    import __graft_entry__
+    __graft_entry__.build()
+    import webgpu_bfs_gb300 as m
+    if args.ncu_case == "materialize":
+        spec = dict(kind="rmat", scale=21, ef=16, S=512, seed=20221)
+    g = make_graph(m, spec)
+    src = m.sample_sources(g, spec["S"], spec["seed"], min_degree=1)
+    eng = m.GpuBfsEngine(m.GpuBfsMethod.Auto)
+    if args.ncu_case == "level":
+        eng.run_ms_reachability(g, src)
+        print("ncu case ok", json.dumps(eng.last_stats))
+    else:
+        import torch
+        out = torch.empty(spec["S"] * g.num_vertices, dtype=torch.int32, device="cuda")
+        eng.run_ms_bfs_device(g, src, out.data_ptr())
+        print("ncu case ok", json.dumps(eng.synchronize()))
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -390,9 +412,16 @@ def main():
     ap.add_argument("--workload", default="rmat22_s512", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", choices=["level", "materialize"],
+                    help="one untimed run sized for an ncu capture: 'level' = the "
+                         "workload in reachability mode (no S*V matrix) with the level "
+                         "loop driven from the host so each level is a plain launch; "
+                         "'materialize' = R-MAT scale 21, S=512, one distance run")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
-    if args.impl == "reference":
+    if args.ncu_case:
+        run_ncu_case(args, spec)
+    elif args.impl == "reference":
         run_reference(args, spec)
     else:
         run_ours(args, spec)

@@ -127,6 +127,7 @@ struct msbfs_engine {
   uint32_t split = 256;
   uint32_t bits_div = 64;
   bool host_loop = false;
+  bool zero_copy = true;  // MSBFS_ZERO_COPY=0 stages host output in HBM instead
   int profiling = 0;
   std::vector<msbfs_level_record> log;       // records of the last call
   LevelRec* h_log = nullptr;                 // pinned, LOG_CAP per pass
@@ -774,6 +775,24 @@ int run_host(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t
   if (S == 0) return MSBFS_OK;
   if (!out) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "out is null");
   CK(cudaSetDevice(eng->device));
+  // Page-locked host output (cudaHostAlloc / cudaHostRegister) is written by
+  // the materialise kernel directly over the host link, in 512-byte row
+  // segments, instead of being staged in HBM and copied afterwards. The
+  // CTA-per-source path stores 4-byte distances as it discovers them, which
+  // the host link serves ~9x slower than a staged copy, so it keeps staging.
+  const bool cta = method_path(resolve_method(g, method, S)) == MSBFS_PATH_CTA &&
+                   cta_max_vertices(eng->device) >= g->V;
+  if (eng->zero_copy && !cta) {
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
+        attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+      if ((rc = enqueue_call(eng, method, g, sources, S, (uint32_t*)attr.devicePointer, nullptr,
+                             nullptr, nullptr)))
+        return rc;
+      return finish_call(eng, stats);
+    }
+    cudaGetLastError();
+  }
   const size_t total = S * g->V;
   if ((rc = grow(eng, &eng->d_dist, &eng->d_dist_cap, total))) return rc;
   if ((rc = enqueue_call(eng, method, g, sources, S, eng->d_dist, nullptr, out, nullptr)))
@@ -814,6 +833,8 @@ int msbfs_engine_create(int device, int method, msbfs_engine** out) {
   e->stream = e->own_stream;
   const char* hl = getenv("MSBFS_HOST_LOOP");
   e->host_loop = hl && hl[0] == '1';
+  const char* zc = getenv("MSBFS_ZERO_COPY");
+  e->zero_copy = !(zc && zc[0] == '0');
   *out = eng.release();
   return MSBFS_OK;
 }
