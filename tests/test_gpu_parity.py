@@ -195,3 +195,20 @@ def test_host_loop_fallback(native, oracle, monkeypatch):
         assert_same(got, _oracle(oracle, g, src), g, src, "host loop")
     finally:
         eng.close()
+
+
+def test_page_locked_host_output(native, oracle):
+    """Level-path output written straight into page-locked host memory."""
+    torch = pytest.importorskip("torch")
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.Auto)
+    try:
+        for g, S in ((native.generate_graph500_rmat(12, 16, 51), 700),
+                     (native.wilson_grid(40, 40, 30, 6), 70)):
+            src = np.random.default_rng(S).integers(0, g.num_vertices, S).astype(np.uint32)
+            pinned = torch.empty(S * g.num_vertices, dtype=torch.int32, pin_memory=True)
+            out = pinned.numpy().view(np.uint32)
+            out[:] = 7
+            eng.run_ms_bfs_into(g, src, out)
+            assert_same(out, _oracle(oracle, g, src), g, src, f"pinned/V={g.num_vertices}")
+    finally:
+        eng.close()
