@@ -38,6 +38,8 @@ WORKLOADS = {
     "road_s256": dict(kind="road", w=339, h=338, extra=5000, S=256, seed=1442),
     "road_s1": dict(kind="road", w=339, h=338, extra=5000, S=1, seed=1442),
     "grid64_s64": dict(kind="grid", w=64, h=64, S=64, seed=64),
+    # 1,000 graphs in one persistent launch (batched form)
+    "batched1000": dict(kind="batched", n_er=600, n_grid=300, n_rmat=100, seed=4040),
 }
 L2_BYTES = 129 * 2**20
 
@@ -381,6 +383,76 @@ def run_ours(args, spec):
         dist.destroy_process_group()
 
 
+def make_batch(m, spec):
+    """Seeded synthetic stand-in for the batched configuration: ER graphs with
+    |V| log-uniform in [1k, 64k] and average degree 8, uniform spanning trees
+    (Wilson) of k x k grids, k in [32, 256], plus 2% extra grid edges, R-MAT
+    scale 16 edge factor 8; each graph gets S log-uniform in [1, 256] sources."""
+    rng = np.random.default_rng(spec["seed"])
+    graphs = []
+    for i in range(spec["n_er"]):
+        n = int(round(np.exp(rng.uniform(np.log(1000), np.log(65536)))))
+        graphs.append(m.generate_erdos_renyi_np(n, 8.0 / (n - 1), spec["seed"] + i))
+    for i in range(spec["n_grid"]):
+        k = int(rng.integers(32, 257))
+        graphs.append(m.wilson_grid(k, k, max(1, round(0.02 * (k * k - 1))),
+                                    spec["seed"] + 10000 + i))
+    for i in range(spec["n_rmat"]):
+        graphs.append(m.generate_graph500_rmat(16, 8, spec["seed"] + 20000 + i))
+    items = []
+    for g in graphs:
+        S = int(np.floor(np.exp(rng.uniform(0, np.log(257)))))
+        S = max(1, min(256, S))
+        items.append((g, rng.integers(0, g.num_vertices, S).astype(np.uint32)))
+    return items
+
+
+def run_batched(args, spec):
+    """Batched form vs the plain per-graph launch loop, both device-timed."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import webgpu_bfs_gb300 as m
+    t0 = time.perf_counter()
+    items = make_batch(m, spec)
+    gen_s = time.perf_counter() - t0
+    total_src = sum(int(s.size) for _, s in items)
+    total_v = sum(g.num_vertices for g, _ in items)
+    b = m.BatchedBfs(items)
+    t0 = time.perf_counter()
+    b.autotune(samples_per_class=3)
+    tune_s = time.perf_counter() - t0
+    for _ in range(max(1, args.warmup)):
+        b.run()
+        b.run_per_graph()
+    steps = max(1, min(args.steps, 10))
+    with ClockSampler(0) as clk:
+        batched = [b.run() for _ in range(steps)]
+    plain = [b.run_per_graph() for _ in range(steps)]
+    ms_b, ms_p = statistics.median(batched), statistics.median(plain)
+    classes = {}
+    for i in range(len(items)):
+        c = b.config(i)
+        classes[c["class"]] = {k: c[k] for k in ("alg", "words", "param")}
+    res = {
+        "metric": "batched MS-BFS sources/sec (1,000 graphs, one launch)",
+        "value": total_src / (ms_b / 1000.0), "unit": "sources/s", "n_gpus": 1,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": ms_b,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "graphs": len(items), "sources": total_src,
+                   "vertices": total_v, "generation_s": round(gen_s, 1),
+                   "autotune_s": round(tune_s, 2), "classes": classes},
+        "plain_per_graph": {"value": total_src / (ms_p / 1000.0), "ms_per_step": ms_p},
+        "speedup_vs_plain": ms_p / ms_b,
+        "p50_ms": ms_b, "p99_ms": float(np.percentile(batched, 99)),
+        "clocks": clk.summary(),
+        "gpu_launches": 1,
+    }
+    print(json.dumps(res), flush=True)
+    b.close()
+
+
 def run_ncu_case(args, spec):
     """A single small invocation for ncu captures (few GB on the device)."""
     os.environ["MSBFS_HOST_LOOP"] = "1"
@@ -421,6 +493,8 @@ def main():
     spec = WORKLOADS[args.workload]
     if args.ncu_case:
         run_ncu_case(args, spec)
+    elif spec["kind"] == "batched" and args.impl != "reference":
+        run_batched(args, spec)
     elif args.impl == "reference":
         run_reference(args, spec)
     else:

@@ -320,6 +320,48 @@ int msbfs_gen_wilson_grid(size_t width, size_t height, size_t extra_edges,
 int msbfs_sample_sources(const msbfs_csr *csr, size_t count, uint64_t seed,
                          uint32_t min_degree, uint32_t *out);
 
+/* ===================== batched form (many graphs, one launch) =============
+ * No single reference counterpart: the reference traverses one graph per
+ * GpuBfsEngine call (engine.rs:219) with fixed method thresholds
+ * (engine.rs:157-198). A batch uploads many graphs with their sources once;
+ * msbfs_batch_run traverses all of them in ONE persistent kernel launch that
+ * pulls (graph, source range) items from a device work list. Per graph class
+ * (road-like / mesh / power-law x vertex-count bucket) the autotuner times
+ * candidate configurations (block-synchronous bit-parallel BFS with 1-8
+ * words per vertex and three bottom-up thresholds, or one single-source BFS
+ * per source with 1/4/16 sources per item) on sample graphs of that class
+ * and caches the fastest, optionally in a text file. Results (S*V u32 per
+ * graph, same bytes as msbfs_run_ms_bfs) stay in device memory until read. */
+#define MSBFS_BATCH_MAX_VERTICES 262144u
+typedef struct msbfs_batch msbfs_batch;
+typedef struct msbfs_batch_graph {
+  size_t num_vertices;
+  size_t num_edges;
+  const uint32_t *row_offsets; /* CSR, validated like CsrGraph::validate */
+  const uint32_t *col_indices;
+  const uint32_t *sources;     /* host, each < num_vertices */
+  size_t num_sources;
+} msbfs_batch_graph;
+int msbfs_batch_create(int device, const msbfs_batch_graph *graphs, size_t num_graphs,
+                       msbfs_batch **out);
+void msbfs_batch_destroy(msbfs_batch *batch);
+int msbfs_batch_autotune(msbfs_batch *batch, size_t samples_per_class,
+                         const char *cache_path);
+/* One persistent launch over every graph; device time in *gpu_ms. */
+int msbfs_batch_run(msbfs_batch *batch, double *gpu_ms);
+/* The plain comparison: one msbfs_run_ms_bfs_device call per graph (Auto
+ * method), same outputs; `graphs` must be the array given at creation. */
+int msbfs_batch_run_per_graph(msbfs_batch *batch, const msbfs_batch_graph *graphs,
+                              double *gpu_ms);
+/* Copies graph i's S*V distance rows to host memory. */
+int msbfs_batch_result(msbfs_batch *batch, size_t graph_index, uint32_t *out);
+/* The tuned configuration of graph i's class: alg 0 = bit-parallel block
+ * (words = max words per vertex, param = bottom-up divisor), 1 = one source
+ * per BFS (param = sources per item). */
+int msbfs_batch_config(const msbfs_batch *batch, size_t graph_index, uint32_t *alg,
+                       uint32_t *words, uint32_t *param, char *class_name,
+                       size_t class_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -512,6 +512,80 @@ class GpuBfsEngine:
         return out.value
 
 
+class BatchedBfs:
+    """Many graphs of uneven size, each with its own sources, traversed in one
+    persistent launch (msbfs_batch_*). ``items`` is a sequence of
+    ``(CsrGraph, sources)``. Results stay on the device until ``result(i)``."""
+
+    ALG_NAMES = {0: "bit_parallel_block", 1: "source_per_bfs"}
+
+    def __init__(self, items, device: int = 0):
+        self._keep = []
+        arr = (_native.BatchGraph * max(1, len(items)))()
+        for i, (g, src) in enumerate(items):
+            s = _u32(src)
+            self._keep.append((g, s))
+            arr[i].num_vertices = g.num_vertices
+            arr[i].num_edges = g.num_edges
+            arr[i].row_offsets = _ptr(g.row_offsets)
+            arr[i].col_indices = _ptr(g.col_indices)
+            arr[i].sources = _ptr(s)
+            arr[i].num_sources = s.size
+        self._arr = arr
+        self._n = len(items)
+        h = C.c_void_p()
+        _check(_native.lib().msbfs_batch_create(device, C.cast(arr, C.c_void_p), self._n,
+                                                C.byref(h)), "msbfs_batch_create failed")
+        self._h = h
+
+    def __len__(self):
+        return self._n
+
+    def autotune(self, samples_per_class: int = 3, cache_path: Optional[str] = None) -> None:
+        _check(_native.lib().msbfs_batch_autotune(
+            self._h, samples_per_class, cache_path.encode() if cache_path else None),
+            "autotune failed")
+
+    def run(self) -> float:
+        """One persistent launch over every graph; returns device ms."""
+        ms = C.c_double()
+        _check(_native.lib().msbfs_batch_run(self._h, C.byref(ms)), "batch run failed")
+        return ms.value
+
+    def run_per_graph(self) -> float:
+        """The plain path: one engine call per graph; returns device ms."""
+        ms = C.c_double()
+        _check(_native.lib().msbfs_batch_run_per_graph(self._h, C.cast(self._arr, C.c_void_p),
+                                                       C.byref(ms)), "per-graph run failed")
+        return ms.value
+
+    def result(self, i: int) -> np.ndarray:
+        g, s = self._keep[i]
+        out = np.empty(s.size * g.num_vertices, np.uint32)
+        if out.size:
+            _check(_native.lib().msbfs_batch_result(self._h, i, _ptr(out)), "result failed")
+        return out
+
+    def config(self, i: int) -> dict:
+        a, w, prm = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        name = C.create_string_buffer(64)
+        _check(_native.lib().msbfs_batch_config(self._h, i, C.byref(a), C.byref(w),
+                                                C.byref(prm), name, 64))
+        return {"class": name.value.decode(), "alg": self.ALG_NAMES.get(a.value, a.value),
+                "words": w.value, "param": prm.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _native.lib().msbfs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------ generators
 GRAPH500_A, GRAPH500_B, GRAPH500_C, GRAPH500_D = 0.57, 0.19, 0.19, 0.05
 

@@ -67,6 +67,17 @@ class Csr(C.Structure):
     ]
 
 
+class BatchGraph(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_size_t),
+        ("num_edges", C.c_size_t),
+        ("row_offsets", u32p),
+        ("col_indices", u32p),
+        ("sources", u32p),
+        ("num_sources", C.c_size_t),
+    ]
+
+
 # name -> (restype, argtypes); every function declared in include/msbfs.h.
 SIGNATURES = {
     "msbfs_engine_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
@@ -98,6 +109,14 @@ SIGNATURES = {
                                                u64p]),
     "msbfs_run_cta_noalloc": (C.c_int, [C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, u32p,
                                         C.c_size_t, C.c_void_p, C.c_void_p]),
+    "msbfs_batch_create": (C.c_int, [C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
+    "msbfs_batch_destroy": (None, [C.c_void_p]),
+    "msbfs_batch_autotune": (C.c_int, [C.c_void_p, C.c_size_t, C.c_char_p]),
+    "msbfs_batch_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "msbfs_batch_run_per_graph": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "msbfs_batch_result": (C.c_int, [C.c_void_p, C.c_size_t, u32p]),
+    "msbfs_batch_config": (C.c_int, [C.c_void_p, C.c_size_t, u32p, u32p, u32p, C.c_char_p,
+                                     C.c_size_t]),
     "msbfs_csr_free": (None, [C.POINTER(Csr)]),
     "msbfs_csr_from_edge_list": (C.c_int, [C.c_size_t, C.c_size_t, u32p, u32p,
                                            C.POINTER(Csr)]),
