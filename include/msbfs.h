@@ -212,6 +212,66 @@ int msbfs_run_ms_bfs_device(msbfs_engine *engine, int method,
                             size_t num_sources, uint32_t *out_device);
 int msbfs_engine_synchronize(msbfs_engine *engine, msbfs_stats *stats);
 
+/* Per-source reductions instead of distance rows (served form output; no
+ * reference counterpart): eccentricity = largest finite distance, reached =
+ * vertices with a finite distance (the source included), distance_sum = sum
+ * of finite distances. Computed on the device from the traversal state; the
+ * S*V matrix is never formed. */
+typedef struct msbfs_source_stats {
+  uint64_t distance_sum;
+  uint32_t eccentricity;
+  uint32_t reached;
+} msbfs_source_stats;
+/* Device output, queued without waiting (msbfs_engine_synchronize waits). */
+int msbfs_run_ms_bfs_stats_device(msbfs_engine *engine, int method,
+                                  const msbfs_graph *graph, const uint32_t *sources,
+                                  size_t num_sources,
+                                  msbfs_source_stats *stats_device);
+/* Host output, blocking, engine's method. */
+int msbfs_run_ms_bfs_stats(msbfs_engine *engine, const msbfs_graph *graph,
+                           const uint32_t *sources, size_t num_sources,
+                           msbfs_source_stats *out, msbfs_stats *stats);
+
+/* ===================== served form (resident graph, request stream) ======
+ * No reference counterpart (the reference is one blocking call per query).
+ * A server keeps the graph resident and runs `slots` traversals at once,
+ * each on its own engine and stream. A scheduler thread packs queued
+ * requests of the same output mode into the next free slot's launch --
+ * unrelated requests share the source lanes of one traversal -- so requests
+ * arriving while others run are admitted as slots free up and their work
+ * overlaps on the device. Admission is by device bytes: each slot's
+ * traversal state is allocated once, and distance rows are staged in at most
+ * hbm_budget_bytes / slots per slot, so a request needing more rows than a
+ * slot can stage is split across launches. Every result is the same bytes
+ * as a lone msbfs_run_ms_bfs / msbfs_run_ms_bfs_stats call. */
+#define MSBFS_SERVE_ROWS 0  /* out = S*V u32 distance rows          */
+#define MSBFS_SERVE_STATS 1 /* out = S msbfs_source_stats           */
+typedef struct msbfs_server msbfs_server;
+typedef struct msbfs_server_config {
+  uint32_t slots;                  /* traversals in flight (0 -> 2)            */
+  uint32_t max_sources_per_launch; /* lanes packed per launch (0 -> 512)       */
+  uint64_t hbm_budget_bytes;       /* row staging, all slots (0 -> 8 GiB)      */
+  int method;                      /* engine method (MSBFS_METHOD_AUTO)        */
+} msbfs_server_config;
+typedef struct msbfs_request_info {
+  double latency_ms; /* submit -> result in host memory       */
+  double queue_ms;   /* submit -> first launch                */
+  uint32_t launches; /* launches the request was split into   */
+  int status;        /* MSBFS_OK or an error code             */
+} msbfs_request_info;
+int msbfs_server_create(int device, size_t num_vertices, size_t num_edges,
+                        const uint32_t *row_offsets, const uint32_t *col_indices,
+                        const msbfs_server_config *config, msbfs_server **out);
+/* Queues a request; `sources` is copied, `out` (host, S*V u32 or S stats)
+ * must stay valid until the request completes. Returns a ticket. */
+int msbfs_server_submit(msbfs_server *server, const uint32_t *sources,
+                        size_t num_sources, int mode, void *out, uint64_t *ticket);
+/* Waits for a ticket (timeout_ms < 0: forever); MSBFS_ERR_TIMEOUT if it
+ * did not complete in time. The ticket is released once it has completed. */
+int msbfs_server_wait(msbfs_server *server, uint64_t ticket, double timeout_ms,
+                      msbfs_request_info *info);
+void msbfs_server_destroy(msbfs_server *server);
+
 /* GpuBfsEngine::run_ms_reachability (engine.rs:420-479): HOST words of
  * V * ceil(S/32) u32, words[v * wpv + s / 32] bit (s % 32) set iff v is
  * reachable from sources[s] (ReachabilityBitmask, graph.rs:446-452). */

@@ -1,0 +1,123 @@
+"""Per-source reductions and the served form (GPU).
+
+The served form packs unrelated requests into the source lanes of shared
+traversals; each request's result must be the same bytes alone and in the
+mix, and equal to the CPU oracle.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from conftest import assert_same
+
+pytestmark = pytest.mark.gpu
+
+MAX = 0xFFFFFFFF
+
+
+def _oracle_stats(oracle, g, src):
+    d = oracle.ms_bfs_fifo(g.num_vertices, g.row_offsets, g.col_indices, src)
+    d = d.reshape(len(src), g.num_vertices).astype(np.int64)
+    fin = d != MAX
+    out = np.zeros(len(src), [("distance_sum", "<u8"), ("eccentricity", "<u4"),
+                              ("reached", "<u4")])
+    out["distance_sum"] = np.where(fin, d, 0).sum(1)
+    out["eccentricity"] = np.where(fin, d, 0).max(1)
+    out["reached"] = fin.sum(1)
+    return out
+
+
+def _same_stats(got, want, label):
+    for f in ("distance_sum", "eccentricity", "reached"):
+        assert np.array_equal(got[f], want[f]), f"{label}: field {f} differs"
+
+
+@pytest.mark.parametrize("method", ["Auto", "PushPullAdaptive", "MultiWordBitParallel",
+                                    "WorkgroupPersistentBfs"])
+def test_source_stats_match_oracle(native, oracle, method):
+    eng = native.GpuBfsEngine(native.GpuBfsMethod[method])
+    try:
+        cases = [(native.generate_graph500_rmat(12, 16, 61), 700),
+                 (native.wilson_grid(50, 40, 40, 7), 300),
+                 (native.path_graph(1500), 5),  # levels beyond the 8 planes
+                 (native.generate_rmat(10, 8, 0.57, 0.19, 0.19, 0.05, 8, directed=True), 40)]
+        for g, S in cases:
+            src = np.random.default_rng(S).integers(0, g.num_vertices, S).astype(np.uint32)
+            got = eng.run_ms_bfs_stats(g, src)
+            _same_stats(got, _oracle_stats(oracle, g, src), f"{method} V={g.num_vertices}")
+    finally:
+        eng.close()
+
+
+def _requests(rng, V, n):
+    sizes = [1, 8, 64, 512, 2048]
+    out = []
+    for i in range(n):
+        S = sizes[int(rng.integers(0, len(sizes)))]
+        mode = int(rng.integers(0, 2))
+        out.append((rng.integers(0, V, S).astype(np.uint32), mode))
+    return out
+
+
+@pytest.mark.parametrize("graph_kind", ["rmat", "road"])
+def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind):
+    torch = pytest.importorskip("torch")
+    if graph_kind == "rmat":
+        g = native.generate_graph500_rmat(12, 8, 71)
+    else:
+        g = native.wilson_grid(60, 60, 72, 8)
+    V = g.num_vertices
+    rng = np.random.default_rng(3)
+    reqs = _requests(rng, V, 14)
+    srv = native.BfsServer(g, slots=2, max_sources_per_launch=512,
+                           hbm_budget_bytes=2 * 300 * V * 4)  # forces row splitting
+    try:
+        # in the mix: submitted from two threads, interleaved
+        tickets = [None] * len(reqs)
+
+        def client(idx):
+            for i in idx:
+                src, mode = reqs[i]
+                out = None
+                if mode == srv.ROWS and i % 3 == 0:  # some outputs page-locked
+                    out = torch.empty(src.size * V, dtype=torch.int32,
+                                      pin_memory=True).numpy().view(np.uint32)
+                tickets[i] = srv.submit(src, mode, out)
+
+        th = [threading.Thread(target=client, args=(list(range(k, len(reqs), 2)),))
+              for k in range(2)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        mixed = []
+        for i, t in enumerate(tickets):
+            res, info = srv.wait(t)
+            assert info["status"] == 0 and info["latency_ms"] >= info["queue_ms"] >= 0
+            mixed.append(res.copy())
+        # alone: one request at a time through the same server
+        for i, (src, mode) in enumerate(reqs):
+            res, _ = srv.wait(srv.submit(src, mode))
+            if mode == srv.ROWS:
+                assert_same(res, mixed[i], g, src, f"request {i} alone vs mix")
+                want = oracle.ms_bfs_fifo(V, g.row_offsets, g.col_indices, src)
+                assert_same(res, want, g, src, f"request {i} vs oracle")
+            else:
+                assert res.tobytes() == mixed[i].tobytes(), f"request {i} stats alone vs mix"
+                _same_stats(res, _oracle_stats(oracle, g, src), f"request {i} stats")
+    finally:
+        srv.close()
+
+
+def test_server_wait_timeout_and_empty(native):
+    g = native.generate_graph500_rmat(10, 8, 5)
+    srv = native.BfsServer(g, slots=1)
+    try:
+        t = srv.submit(np.zeros(0, np.uint32), srv.STATS)
+        res, info = srv.wait(t)
+        assert res.size == 0 and info["launches"] == 0
+        with pytest.raises(native.BfsError):
+            srv.submit(np.array([g.num_vertices], np.uint32), srv.STATS)
+    finally:
+        srv.close()

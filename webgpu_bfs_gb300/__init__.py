@@ -512,6 +512,87 @@ class GpuBfsEngine:
         return out.value
 
 
+SOURCE_STATS_DTYPE = np.dtype(_native.SOURCE_STATS_DTYPE)
+
+
+def _engine_run_ms_bfs_stats(self, graph: "CsrGraph", sources) -> np.ndarray:
+    """Per-source eccentricity / reached count / distance sum, computed on the
+    device without forming the S*V matrix (msbfs_run_ms_bfs_stats)."""
+    src = _u32(sources)
+    out = np.zeros(src.size, SOURCE_STATS_DTYPE)
+    if src.size == 0:
+        return out
+    dg = self.upload(graph)
+    st = Stats()
+    rc = _native.lib().msbfs_run_ms_bfs_stats(self._h, dg.handle, _ptr(src), src.size,
+                                              out.ctypes.data_as(C.c_void_p), C.byref(st))
+    self._check(rc)
+    self.last_stats = st.as_dict()
+    return out
+
+
+GpuBfsEngine.run_ms_bfs_stats = _engine_run_ms_bfs_stats
+
+
+class ServerTicket:
+    __slots__ = ("id", "out", "mode", "sources")
+
+    def __init__(self, tid, out, mode, sources):
+        self.id, self.out, self.mode, self.sources = tid, out, mode, sources
+
+
+class BfsServer:
+    """Served form (msbfs_server_*): a resident graph, a request queue and a
+    scheduler that packs requests into shared traversals on ``slots``
+    concurrent engines. ``submit`` returns at once; ``wait`` returns the
+    result (rows: u32 array of S*V; stats: SOURCE_STATS_DTYPE array) and the
+    request's latency record."""
+
+    ROWS, STATS = 0, 1
+
+    def __init__(self, graph: "CsrGraph", slots: int = 2, max_sources_per_launch: int = 512,
+                 hbm_budget_bytes: int = 0, method: GpuBfsMethod = GpuBfsMethod.Auto,
+                 device: int = 0):
+        cfg = _native.ServerConfig(slots, max_sources_per_launch, hbm_budget_bytes, int(method))
+        h = C.c_void_p()
+        self.graph = graph
+        self.V = graph.num_vertices
+        _check(_native.lib().msbfs_server_create(device, graph.num_vertices, graph.num_edges,
+                                                 _ptr(graph.row_offsets),
+                                                 _ptr(graph.col_indices), C.byref(cfg),
+                                                 C.byref(h)), "msbfs_server_create failed")
+        self._h = h
+
+    def submit(self, sources, mode: int = STATS, out: Optional[np.ndarray] = None) -> ServerTicket:
+        src = _u32(sources)
+        if out is None:
+            out = (np.empty(src.size * self.V, np.uint32) if mode == self.ROWS
+                   else np.zeros(src.size, SOURCE_STATS_DTYPE))
+        t = C.c_uint64()
+        rc = _native.lib().msbfs_server_submit(self._h, _ptr(src), src.size, int(mode),
+                                               out.ctypes.data_as(C.c_void_p), C.byref(t))
+        _check(rc, "submit failed")
+        return ServerTicket(t.value, out, mode, src)
+
+    def wait(self, ticket: ServerTicket, timeout_ms: float = -1.0):
+        info = _native.RequestInfo()
+        rc = _native.lib().msbfs_server_wait(self._h, ticket.id, float(timeout_ms),
+                                             C.byref(info))
+        _check(rc, "request failed")
+        return ticket.out, info.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _native.lib().msbfs_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class BatchedBfs:
     """Many graphs of uneven size, each with its own sources, traversed in one
     persistent launch (msbfs_batch_*). ``items`` is a sequence of

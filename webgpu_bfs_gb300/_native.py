@@ -67,6 +67,31 @@ class Csr(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("slots", C.c_uint32),
+        ("max_sources_per_launch", C.c_uint32),
+        ("hbm_budget_bytes", C.c_uint64),
+        ("method", C.c_int),
+    ]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [
+        ("latency_ms", C.c_double),
+        ("queue_ms", C.c_double),
+        ("launches", C.c_uint32),
+        ("status", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+# numpy view of msbfs_source_stats
+SOURCE_STATS_DTYPE = [("distance_sum", "<u8"), ("eccentricity", "<u4"), ("reached", "<u4")]
+
+
 class BatchGraph(C.Structure):
     _fields_ = [
         ("num_vertices", C.c_size_t),
@@ -109,6 +134,17 @@ SIGNATURES = {
                                                u64p]),
     "msbfs_run_cta_noalloc": (C.c_int, [C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, u32p,
                                         C.c_size_t, C.c_void_p, C.c_void_p]),
+    "msbfs_run_ms_bfs_stats_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, u32p,
+                                                C.c_size_t, C.c_void_p]),
+    "msbfs_run_ms_bfs_stats": (C.c_int, [C.c_void_p, C.c_void_p, u32p, C.c_size_t, C.c_void_p,
+                                         C.POINTER(Stats)]),
+    "msbfs_server_create": (C.c_int, [C.c_int, C.c_size_t, C.c_size_t, u32p, u32p,
+                                      C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "msbfs_server_submit": (C.c_int, [C.c_void_p, u32p, C.c_size_t, C.c_int, C.c_void_p,
+                                      C.POINTER(C.c_uint64)]),
+    "msbfs_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double,
+                                    C.POINTER(RequestInfo)]),
+    "msbfs_server_destroy": (None, [C.c_void_p]),
     "msbfs_batch_create": (C.c_int, [C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
     "msbfs_batch_destroy": (None, [C.c_void_p]),
     "msbfs_batch_autotune": (C.c_int, [C.c_void_p, C.c_size_t, C.c_char_p]),

@@ -25,32 +25,40 @@ __global__ void cta_bfs_kernel(CtaParams p) {
   extern __shared__ uint32_t bitmap[];
   __shared__ uint32_t s_src_idx;
   __shared__ uint32_t s_count;
+  __shared__ unsigned long long s_sum;
+  __shared__ uint32_t s_reached;
   const uint32_t V = p.V;
   const uint32_t words = (V + 31) / 32;
-  const uint32_t lane = threadIdx.x & 31;
   uint32_t* qa = p.gqueue + (size_t)blockIdx.x * 2 * V;
   uint32_t* qb = qa + V;
 
   for (;;) {
-    if (threadIdx.x == 0) s_src_idx = atomicAdd(p.work, 1u);
+    if (threadIdx.x == 0) {
+      s_src_idx = atomicAdd(p.work, 1u);
+      s_sum = 0;
+      s_reached = 0;
+    }
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) bitmap[i] = 0;
     __syncthreads();
     const uint32_t si = s_src_idx;
     if (si >= p.num_sources) break;
     const uint32_t src = p.sources[si];
-    uint32_t* row = p.dist + (size_t)si * V;
+    uint32_t* row = p.dist ? p.dist + (size_t)si * V : nullptr;
     if (threadIdx.x == 0) {
       bitmap[src >> 5] = 1u << (src & 31);
-      row[src] = 0;
+      if (row) row[src] = 0;
       qa[0] = src;
       s_count = 0;
     }
     uint32_t n_in = 1;
-    uint32_t level = 0;
+    uint32_t level = 0, ecc = 0;
+    unsigned long long my_sum = 0;
+    uint32_t my_cnt = 0;
     uint32_t* qin = qa;
     uint32_t* qout = qb;
     __syncthreads();
     while (n_in) {
+      ecc = level;
       const uint32_t nd = level + 1;
       // Threads sweep the frontier; each expands one vertex's out-edges.
       const uint32_t n_round = (n_in + blockDim.x - 1) / blockDim.x * blockDim.x;
@@ -64,7 +72,9 @@ __global__ void cta_bfs_kernel(CtaParams p) {
             if (bitmap[v >> 5] & bit) continue;
             const uint32_t old = atomicOr(&bitmap[v >> 5], bit);
             if (old & bit) continue;
-            row[v] = nd;
+            if (row) row[v] = nd;
+            my_sum += nd;
+            ++my_cnt;
             const uint32_t pos = atomicAdd(&s_count, 1u);
             qout[pos] = v;
           }
@@ -80,10 +90,23 @@ __global__ void cta_bfs_kernel(CtaParams p) {
       ++level;
       __syncthreads();
     }
-    // Unreached vertices: coalesced sweep of the row guided by the bitmap.
-    for (uint32_t v = threadIdx.x; v < V; v += blockDim.x)
-      if (!((bitmap[v >> 5] >> (v & 31)) & 1u)) row[v] = CTA_DIST_MAX;
-    (void)lane;
+    if (row) {
+      // Unreached vertices: coalesced sweep of the row guided by the bitmap.
+      for (uint32_t v = threadIdx.x; v < V; v += blockDim.x)
+        if (!((bitmap[v >> 5] >> (v & 31)) & 1u)) row[v] = CTA_DIST_MAX;
+    }
+    if (p.stats) {
+      if (my_cnt) {
+        atomicAdd(&s_sum, my_sum);
+        atomicAdd(&s_reached, my_cnt);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        p.stats[si].sum = s_sum;
+        p.stats[si].reached = s_reached + 1;
+        p.stats[si].ecc = ecc;
+      }
+    }
     __syncthreads();
   }
 }

@@ -82,10 +82,20 @@ struct HeavyChunk {
 
 // Per-pass descriptor, read from device memory so one captured CUDA graph can
 // serve every pass and every call.
+// Per-source reductions of a traversal (served form): eccentricity (largest
+// finite distance), reached vertices (the source included) and the sum of
+// finite distances. Layout shared with msbfs_source_stats in msbfs.h.
+struct SourceStats {
+  unsigned long long sum;
+  uint32_t ecc;
+  uint32_t reached;
+};
+
 struct PassDesc {
   const uint32_t* sources;  // this pass's sources (device)
   uint32_t* dist;           // first row of this pass in the distance matrix
   uint32_t* reach;          // non-null: write visited words here instead
+  SourceStats* stats;       // non-null: per-source reductions instead of rows
   uint32_t num_sources;     // P
   uint32_t reach_wpv;       // words per vertex of the reachability output
   uint32_t reach_col;       // word column of this pass in that output
@@ -153,9 +163,10 @@ struct CtaParams {
   const uint32_t* idx;
   const uint32_t* sources;
   uint32_t num_sources;
-  uint32_t* dist;        // row s at dist + s * V
+  uint32_t* dist;        // row s at dist + s * V (null when stats is set)
   uint32_t* gqueue;      // per resident block: 2 * V u32
   uint32_t* work;        // source cursor (zeroed before launch)
+  SourceStats* stats;    // non-null: per-source reductions instead of rows
 };
 // Max V for the shared-memory visited bitmap; grid/block for the CTA kernel.
 size_t cta_max_vertices(int device);

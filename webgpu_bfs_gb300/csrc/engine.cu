@@ -147,6 +147,8 @@ struct msbfs_engine {
   size_t d_cta_queue_cap = 0;
   uint32_t* d_work = nullptr;
   unsigned long long* d_counter = nullptr;
+  SourceStats* d_sstats = nullptr;  // per-source reductions of host-output calls
+  size_t d_sstats_cap = 0;
   LevelCtl* h_ctl = nullptr;  // pinned, one per pass of the last call
   size_t h_ctl_cap = 0;
   // last call
@@ -487,8 +489,9 @@ int resolve_method(const msbfs_graph* g, int method, size_t S) {
 // copy stream while later passes run.
 int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t* sources,
                  size_t S, uint32_t* dist_dev, uint32_t* reach_dev, uint32_t* host_out,
-                 uint32_t* host_reach) {
+                 uint32_t* host_reach, SourceStats* stats_dev = nullptr) {
   int rc;
+  if (stats_dev) CK(cudaMemsetAsync(stats_dev, 0, S * sizeof(SourceStats), eng->stream));
   const int m = resolve_method(g, method, S);
   uint32_t path = method_path(m);
   if (reach_dev && path == MSBFS_PATH_CTA) path = MSBFS_PATH_HYBRID;
@@ -523,6 +526,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     cp.dist = dist_dev;
     cp.gqueue = eng->d_cta_queue;
     cp.work = eng->d_work;
+    cp.stats = stats_dev;
     launch_cta(cp, std::min<int>(cta_grid, (int)S), cta_block, cta_smem, eng->stream);
     CK(cudaGetLastError());
     eng->last.passes = 1;
@@ -573,6 +577,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     d.sources = eng->d_sources + s0;
     d.dist = dist_dev ? dist_dev + s0 * V : nullptr;
     d.reach = reach_dev;
+    d.stats = stats_dev ? stats_dev + s0 : nullptr;
     d.num_sources = (uint32_t)np;
     d.reach_wpv = (uint32_t)wpv;
     d.reach_col = (uint32_t)(ps * W);
@@ -851,6 +856,7 @@ void msbfs_engine_destroy(msbfs_engine* e) {
   cudaFree(e->d_cta_queue);
   cudaFree(e->d_work);
   cudaFree(e->d_counter);
+  cudaFree(e->d_sstats);
   if (e->h_ctl) cudaFreeHost(e->h_ctl);
   if (e->h_log) cudaFreeHost(e->h_log);
   for (cudaEvent_t ev : e->lvl_events) cudaEventDestroy(ev);
@@ -989,6 +995,52 @@ int msbfs_run_ms_bfs_device(msbfs_engine* e, int method, const msbfs_graph* g,
   if (!out_device) return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "out is null");
   CK(cudaSetDevice(e->device));
   return enqueue_call(e, method, g, sources, S, out_device, nullptr, nullptr, nullptr);
+}
+
+static_assert(sizeof(SourceStats) == sizeof(msbfs_source_stats), "stats layout");
+
+int msbfs_run_ms_bfs_stats_device(msbfs_engine* e, int method, const msbfs_graph* g,
+                                  const uint32_t* sources, size_t S,
+                                  msbfs_source_stats* stats_device) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (method < 0 || method > MSBFS_METHOD_AUTO)
+    return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "unknown method");
+  std::lock_guard<std::mutex> lk(e->mu);
+  msbfs_engine* eng = e;
+  int rc = validate_call(e, g, sources, S);
+  if (rc) return rc;
+  e->last = msbfs_stats{};
+  e->last_passes = 0;
+  if (S == 0) {
+    CK(cudaEventRecord(e->ev_start, e->stream));
+    CK(cudaEventRecord(e->ev_stop, e->stream));
+    return MSBFS_OK;
+  }
+  if (!stats_device) return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "stats is null");
+  CK(cudaSetDevice(e->device));
+  return enqueue_call(e, method, g, sources, S, nullptr, nullptr, nullptr, nullptr,
+                      reinterpret_cast<SourceStats*>(stats_device));
+}
+
+int msbfs_run_ms_bfs_stats(msbfs_engine* e, const msbfs_graph* g, const uint32_t* sources,
+                           size_t S, msbfs_source_stats* out, msbfs_stats* stats) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  msbfs_engine* eng = e;
+  int rc = validate_call(e, g, sources, S);
+  if (rc) return rc;
+  if (stats) *stats = msbfs_stats{};
+  if (S == 0) return MSBFS_OK;
+  if (!out) return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "out is null");
+  CK(cudaSetDevice(e->device));
+  if ((rc = grow(e, &e->d_sstats, &e->d_sstats_cap, S))) return rc;
+  if ((rc = enqueue_call(e, e->method, g, sources, S, nullptr, nullptr, nullptr, nullptr,
+                         e->d_sstats)))
+    return rc;
+  CK(cudaMemcpyAsync(out, e->d_sstats, S * sizeof(SourceStats), cudaMemcpyDeviceToHost,
+                     e->stream));
+  CK(cudaEventRecord(e->ev_stop, e->stream));
+  return finish_call(e, stats);
 }
 
 int msbfs_engine_synchronize(msbfs_engine* e, msbfs_stats* stats) {

@@ -233,17 +233,26 @@ __device__ __forceinline__ void record_level(const LevelParams& p, uint32_t v, u
     }
   } else {
     // Deeper than the planes can encode: mark the lanes and write the rows.
-    uint32_t* dist = p.desc->dist;  // null when only reachability is wanted
+    // With per-source reductions instead of rows, the deep lanes are folded
+    // into the reductions here.
+    uint32_t* dist = p.desc->dist;  // null when reductions or reachability are wanted
+    SourceStats* st = p.desc->stats;
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
       uint32_t bits = newly.w[j];
       if (!bits) continue;
       atomicOr(p.ovf + off + j, bits);
-      while (dist && bits) {
+      while ((dist || st) && bits) {
         const uint32_t t = __ffs(bits) - 1;
         bits &= bits - 1;
         const size_t s = (size_t)(k0 + j) * 32 + t;
-        dist[s * p.V + v] = d;
+        if (dist) {
+          dist[s * p.V + v] = d;
+        } else {
+          atomicAdd(&st[s].sum, (unsigned long long)d);
+          atomicMax(&st[s].ecc, d);
+          atomicAdd(&st[s].reached, 1u);
+        }
       }
     }
   }
@@ -904,6 +913,72 @@ __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint
 // (or copies the visited words out as a reachability bitmask) and zeroes the
 // words it read, so the next pass starts from clean buffers. Warps take
 // (vertex tile, word) items independently: no shared memory, no barriers.
+// Per-source reductions straight from the visited words and level planes
+// (no S*V matrix): a warp item is word c of 1024 consecutive vertices, lane j
+// accumulates source 32c+j, and each lane loads one vertex's words which the
+// warp then walks with shuffles. The words read are zeroed like in the
+// materialisation; lanes flagged in ovf were accumulated by the level kernel.
+template <int W>
+__device__ void reduce_sources(const LevelParams& p, uint32_t P, uint32_t npu, bool use_ovf) {
+  constexpr uint32_t CHUNK = 1024;
+  const uint32_t Wu = (P + 31) / 32;
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t VW = (size_t)p.V * W;
+  SourceStats* st = p.desc->stats;
+  const size_t nitems = (size_t)((p.V + CHUNK - 1) / CHUNK) * Wu;
+  const size_t warp_g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t it = warp_g; it < nitems; it += nwarps) {
+    const uint32_t c = (uint32_t)(it % Wu);
+    const uint32_t v0 = (uint32_t)(it / Wu) * CHUNK;
+    const uint32_t v_end = min(v0 + CHUNK, p.V);
+    unsigned long long sum = 0;
+    uint32_t ecc = 0, cnt = 0;
+    for (uint32_t vb = v0; vb < v_end; vb += 32) {
+      const uint32_t v = vb + lane;
+      uint32_t x = 0, o = 0, pl[MAT_NPMAX];
+#pragma unroll
+      for (int b = 0; b < MAT_NPMAX; ++b) pl[b] = 0;
+      if (v < v_end) {
+        const size_t a = (size_t)v * W + c;
+        x = p.vis[a];
+        p.vis[a] = 0;
+        if (use_ovf) {
+          o = p.ovf[a];
+          p.ovf[a] = 0;
+        }
+#pragma unroll
+        for (int b = 0; b < MAT_NPMAX; ++b)
+          if (b < (int)npu) {
+            pl[b] = p.planes[b * VW + a];
+            p.planes[b * VW + a] = 0;
+          }
+      }
+      uint32_t live = __ballot_sync(FULL, x != 0);
+      while (live) {
+        const int t = __ffs(live) - 1;
+        live &= live - 1;
+        const uint32_t xt = __shfl_sync(FULL, x, t) & ~__shfl_sync(FULL, o, t);
+        uint32_t d = 0;
+#pragma unroll
+        for (int b = 0; b < MAT_NPMAX; ++b)
+          if (b < (int)npu) d |= ((__shfl_sync(FULL, pl[b], t) >> lane) & 1u) << b;
+        if ((xt >> lane) & 1u) {
+          sum += d;
+          ecc = max(ecc, d);
+          ++cnt;
+        }
+      }
+    }
+    if (cnt && 32 * c + lane < P) {
+      SourceStats* s = st + 32 * c + lane;
+      atomicAdd(&s->sum, sum);
+      atomicMax(&s->ecc, ecc);
+      atomicAdd(&s->reached, cnt);
+    }
+  }
+}
+
 template <int W>
 __global__ void __launch_bounds__(MAT_BLOCK, 4) materialize_kernel(LevelParams p) {
   const PassDesc* dsc = p.desc;
@@ -912,6 +987,10 @@ __global__ void __launch_bounds__(MAT_BLOCK, 4) materialize_kernel(LevelParams p
   const uint32_t dmax = p.ctl->level;
   const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
   const bool use_ovf = dmax >= (1u << p.NP);
+  if (dsc->stats) {
+    reduce_sources<W>(p, P, npu, use_ovf);
+    return;
+  }
   const uint32_t lane = threadIdx.x & 31;
   const bool vec_ok = (p.V % 4 == 0) && (((uintptr_t)dsc->dist & 15) == 0);
   const size_t ntiles = (p.V + MAT_TV - 1) / MAT_TV;

@@ -1,0 +1,351 @@
+// Served form: a resident graph, a request queue and a scheduler thread that
+// packs queued requests into the source lanes of shared traversals running
+// on several slots (engines/streams) at once. See include/msbfs.h ("served
+// form") for the contract. No reference counterpart: the reference answers
+// one blocking query per call (crates/gpu_bfs/src/engine.rs:219-298).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/msbfs.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  uint64_t id = 0;
+  std::vector<uint32_t> src;
+  int mode = MSBFS_SERVE_STATS;
+  void* out = nullptr;
+  bool out_pinned = false;   // device-visible page-locked host memory
+  size_t next = 0;           // first source not yet given to a launch
+  size_t in_flight = 0;      // launches of this request still running
+  uint32_t launches = 0;
+  bool launched = false;
+  bool done = false;
+  int status = MSBFS_OK;
+  Clock::time_point submit, first_launch, complete;
+};
+
+struct Part {
+  Request* r;
+  size_t src_off;   // first source of the request in this launch
+  size_t n;
+  size_t lane_off;  // its first lane in the launch
+};
+
+struct Slot {
+  msbfs_engine* eng = nullptr;
+  msbfs_graph* g = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev = nullptr;
+  uint32_t* d_rows = nullptr;
+  size_t rows_cap = 0;  // sources whose rows fit the slot's staging
+  msbfs_source_stats* d_stats = nullptr;
+  void* h_stage = nullptr;  // page-locked bounce buffer for pageable outputs
+  size_t h_stage_bytes = 0;
+  std::vector<Part> parts;
+  int mode = MSBFS_SERVE_STATS;
+  bool busy = false;
+  int launch_rc = MSBFS_OK;
+};
+
+size_t elem_bytes(int mode, size_t V) {
+  return mode == MSBFS_SERVE_ROWS ? V * sizeof(uint32_t) : sizeof(msbfs_source_stats);
+}
+
+}  // namespace
+
+struct msbfs_server {
+  int device = 0;
+  size_t V = 0;
+  msbfs_server_config cfg{};
+  std::vector<Slot> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request*> queue;
+  std::map<uint64_t, std::unique_ptr<Request>> reqs;
+  uint64_t next_id = 1;
+  bool stop = false;
+  std::thread sched;
+};
+
+namespace {
+
+void finish_part(msbfs_server* s, const Part& p, int rc) {
+  Request* r = p.r;
+  if (rc && !r->status) r->status = rc;
+  if (--r->in_flight == 0 && r->next == r->src.size()) {
+    r->done = true;
+    r->complete = Clock::now();
+    s->cv_done.notify_all();
+  }
+}
+
+// Issues one launch on slot `sl` (called without the lock; the slot is busy
+// so only the scheduler touches it).
+int launch_slot(msbfs_server* s, Slot& sl, const std::vector<uint32_t>& lanes) {
+  const size_t V = s->V, n = lanes.size();
+  const size_t eb = elem_bytes(sl.mode, V);
+  int rc;
+  if (sl.mode == MSBFS_SERVE_ROWS)
+    rc = msbfs_run_ms_bfs_device(sl.eng, s->cfg.method, sl.g, lanes.data(), n, sl.d_rows);
+  else
+    rc = msbfs_run_ms_bfs_stats_device(sl.eng, s->cfg.method, sl.g, lanes.data(), n,
+                                       sl.d_stats);
+  if (rc) return rc;
+  bool need_stage = false;
+  for (const Part& p : sl.parts) need_stage |= !p.r->out_pinned;
+  if (need_stage && sl.h_stage_bytes < n * eb) {
+    if (sl.h_stage) cudaFreeHost(sl.h_stage);
+    sl.h_stage = nullptr;
+    sl.h_stage_bytes = 0;
+    if (cudaMallocHost(&sl.h_stage, n * eb) != cudaSuccess) {
+      cudaGetLastError();
+      return MSBFS_ERR_OOM;
+    }
+    sl.h_stage_bytes = n * eb;
+  }
+  const char* dsrc = sl.mode == MSBFS_SERVE_ROWS ? reinterpret_cast<const char*>(sl.d_rows)
+                                                 : reinterpret_cast<const char*>(sl.d_stats);
+  for (const Part& p : sl.parts) {
+    char* dst = p.r->out_pinned ? static_cast<char*>(p.r->out) + p.src_off * eb
+                                : static_cast<char*>(sl.h_stage) + p.lane_off * eb;
+    if (cudaMemcpyAsync(dst, dsrc + p.lane_off * eb, p.n * eb, cudaMemcpyDeviceToHost,
+                        sl.stream) != cudaSuccess) {
+      cudaGetLastError();
+      return MSBFS_ERR_CUDA;
+    }
+  }
+  if (cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return MSBFS_ERR_CUDA;
+  }
+  return MSBFS_OK;
+}
+
+void scheduler(msbfs_server* s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    bool progress = false, any_busy = false;
+    // Completions: results are in host memory once the slot's event fired.
+    for (Slot& sl : s->slots) {
+      if (!sl.busy) continue;
+      int rc = sl.launch_rc;
+      if (!rc) {
+        const cudaError_t q = cudaEventQuery(sl.ev);
+        if (q == cudaErrorNotReady) {
+          any_busy = true;
+          continue;
+        }
+        if (q != cudaSuccess) {
+          cudaGetLastError();
+          rc = MSBFS_ERR_CUDA;
+        }
+      }
+      const size_t eb = elem_bytes(sl.mode, s->V);
+      for (const Part& p : sl.parts) {
+        if (!rc && !p.r->out_pinned)
+          std::memcpy(static_cast<char*>(p.r->out) + p.src_off * eb,
+                      static_cast<char*>(sl.h_stage) + p.lane_off * eb, p.n * eb);
+        finish_part(s, p, rc);
+      }
+      sl.parts.clear();
+      sl.busy = false;
+      progress = true;
+    }
+    // Admissions: the next free slot takes queued requests of the head's
+    // output mode, in arrival order, until its lanes (and, for rows, its
+    // staging bytes) are used up; larger requests continue in later launches.
+    for (Slot& sl : s->slots) {
+      if (sl.busy || s->queue.empty()) continue;
+      sl.mode = s->queue.front()->mode;
+      size_t cap = s->cfg.max_sources_per_launch;
+      if (sl.mode == MSBFS_SERVE_ROWS) cap = std::min(cap, sl.rows_cap);
+      std::vector<uint32_t> lanes;
+      const auto now = Clock::now();
+      for (size_t i = 0; i < s->queue.size() && lanes.size() < cap;) {
+        Request* r = s->queue[i];
+        if (r->mode != sl.mode) {
+          ++i;
+          continue;
+        }
+        const size_t take = std::min(r->src.size() - r->next, cap - lanes.size());
+        sl.parts.push_back(Part{r, r->next, take, lanes.size()});
+        lanes.insert(lanes.end(), r->src.begin() + r->next, r->src.begin() + r->next + take);
+        r->next += take;
+        r->in_flight++;
+        r->launches++;
+        if (!r->launched) {
+          r->launched = true;
+          r->first_launch = now;
+        }
+        if (r->next == r->src.size())
+          s->queue.erase(s->queue.begin() + i);
+        else
+          ++i;
+      }
+      sl.busy = true;
+      any_busy = true;
+      progress = true;
+      lk.unlock();
+      sl.launch_rc = launch_slot(s, sl, lanes);
+      lk.lock();
+    }
+    if (s->stop && s->queue.empty() && !any_busy) break;
+    if (!progress)
+      s->cv_work.wait_for(lk, any_busy ? std::chrono::microseconds(20)
+                                       : std::chrono::microseconds(2000));
+  }
+}
+
+void destroy_slots(msbfs_server* s) {
+  for (Slot& sl : s->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.g) msbfs_graph_destroy(sl.g);
+    if (sl.eng) msbfs_engine_destroy(sl.eng);
+    if (sl.d_rows) cudaFree(sl.d_rows);
+    if (sl.d_stats) cudaFree(sl.d_stats);
+    if (sl.h_stage) cudaFreeHost(sl.h_stage);
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+  }
+  s->slots.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+int msbfs_server_create(int device, size_t V, size_t E, const uint32_t* ro, const uint32_t* ci,
+                        const msbfs_server_config* config, msbfs_server** out) {
+  if (!out) return MSBFS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (V == 0) return MSBFS_ERR_EMPTY_GRAPH;
+  auto s = std::make_unique<msbfs_server>();
+  s->device = device;
+  s->V = V;
+  if (config) s->cfg = *config;
+  if (!config) s->cfg.method = MSBFS_METHOD_AUTO;
+  if (s->cfg.slots == 0) s->cfg.slots = 2;
+  if (s->cfg.max_sources_per_launch == 0) s->cfg.max_sources_per_launch = 512;
+  if (s->cfg.hbm_budget_bytes == 0) s->cfg.hbm_budget_bytes = 8ull << 30;
+  if (s->cfg.method < 0 || s->cfg.method > MSBFS_METHOD_AUTO) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return MSBFS_ERR_NO_DEVICE;
+  }
+  const size_t per_slot = s->cfg.hbm_budget_bytes / s->cfg.slots;
+  const size_t rows_cap =
+      std::max<size_t>(1, std::min<size_t>(s->cfg.max_sources_per_launch, per_slot / (V * 4)));
+  s->slots.resize(s->cfg.slots);
+  int rc = MSBFS_OK;
+  for (Slot& sl : s->slots) {
+    if ((rc = msbfs_engine_create(device, s->cfg.method, &sl.eng))) break;
+    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
+      rc = MSBFS_ERR_CUDA;
+      break;
+    }
+    if ((rc = msbfs_engine_set_stream(sl.eng, sl.stream))) break;
+    if ((rc = msbfs_graph_create(sl.eng, V, E, ro, ci, &sl.g))) break;
+    sl.rows_cap = rows_cap;
+    if (cudaMalloc((void**)&sl.d_rows, rows_cap * V * 4) != cudaSuccess ||
+        cudaMalloc((void**)&sl.d_stats,
+                   s->cfg.max_sources_per_launch * sizeof(msbfs_source_stats)) != cudaSuccess) {
+      cudaGetLastError();
+      rc = MSBFS_ERR_OOM;
+      break;
+    }
+  }
+  if (rc) {
+    destroy_slots(s.get());
+    return rc;
+  }
+  msbfs_server* raw = s.get();
+  s->sched = std::thread(scheduler, raw);
+  *out = s.release();
+  return MSBFS_OK;
+}
+
+int msbfs_server_submit(msbfs_server* s, const uint32_t* sources, size_t S, int mode, void* out,
+                        uint64_t* ticket) {
+  if (!s || !ticket || (S && (!sources || !out))) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (mode != MSBFS_SERVE_ROWS && mode != MSBFS_SERVE_STATS) return MSBFS_ERR_INVALID_ARGUMENT;
+  for (size_t i = 0; i < S; ++i)
+    if ((size_t)sources[i] >= s->V) return MSBFS_ERR_SOURCE_OOB;
+  auto r = std::make_unique<Request>();
+  r->src.assign(sources, sources + S);
+  r->mode = mode;
+  r->out = out;
+  cudaPointerAttributes attr{};
+  if (out && cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
+      attr.type == cudaMemoryTypeHost)
+    r->out_pinned = true;
+  else
+    cudaGetLastError();
+  r->submit = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop) return MSBFS_ERR_INVALID_ARGUMENT;
+  r->id = s->next_id++;
+  *ticket = r->id;
+  if (S == 0) {
+    r->done = true;
+    r->complete = r->first_launch = r->submit;
+  } else {
+    s->queue.push_back(r.get());
+  }
+  s->reqs[r->id] = std::move(r);
+  s->cv_work.notify_one();
+  return MSBFS_OK;
+}
+
+int msbfs_server_wait(msbfs_server* s, uint64_t ticket, double timeout_ms,
+                      msbfs_request_info* info) {
+  if (!s) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return MSBFS_ERR_INVALID_ARGUMENT;
+  Request* r = it->second.get();
+  auto pred = [r] { return r->done; };
+  if (timeout_ms < 0)
+    s->cv_done.wait(lk, pred);
+  else if (!s->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), pred))
+    return MSBFS_ERR_TIMEOUT;
+  const int st = r->status;
+  if (info) {
+    using ms = std::chrono::duration<double, std::milli>;
+    info->latency_ms = ms(r->complete - r->submit).count();
+    info->queue_ms = ms(r->first_launch - r->submit).count();
+    info->launches = r->launches;
+    info->status = st;
+  }
+  s->reqs.erase(it);
+  return st;
+}
+
+void msbfs_server_destroy(msbfs_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->sched.joinable()) s->sched.join();
+  cudaSetDevice(s->device);
+  destroy_slots(s);
+  delete s;
+}
+
+}  // extern "C"
