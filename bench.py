@@ -40,7 +40,17 @@ WORKLOADS = {
     "grid64_s64": dict(kind="grid", w=64, h=64, S=64, seed=64),
     # 1,000 graphs in one persistent launch (batched form)
     "batched1000": dict(kind="batched", n_er=600, n_grid=300, n_rmat=100, seed=4040),
+    # served form: a resident graph answering a Poisson stream of requests
+    # with |S| drawn from {1, 8, 64, 512, 2048}, per-source statistics out
+    "served_rmat24": dict(kind="served", graph=dict(kind="rmat", scale=24, ef=16, seed=24024),
+                          requests=160, seed=5150),
+    "served_road1448": dict(kind="served",
+                            graph=dict(kind="road", w=1448, h=1448, extra=41934, seed=1448),
+                            requests=240, seed=5151),
 }
+SERVED_SIZES = (1, 8, 64, 512, 2048)
+SERVED_CONFIG = dict(slots=4, express_slots=1, small_sources=64, general_sm_percent=85,
+                     max_sources_per_launch=512)
 L2_BYTES = 129 * 2**20
 
 
@@ -53,6 +63,10 @@ def make_graph(m, spec):
 
 
 def workload_config(name, spec, g):
+    if spec["kind"] == "served":
+        return {"workload": name, "graph": spec["graph"], "num_vertices": g.num_vertices,
+                "num_edges": g.num_edges, "requests": spec["requests"],
+                "request_sizes": list(SERVED_SIZES)}
     cfg = {"workload": name, "num_vertices": g.num_vertices, "num_edges": g.num_edges,
            "sources": spec["S"], "source_sampling": "uniform among degree>=1, seeded",
            "graph": spec["kind"]}
@@ -175,8 +189,14 @@ def run_reference(args, spec):
     import webgpu_bfs_gb300 as m
     from oracle import oracle
     oracle.build()
-    g = make_graph(m, spec)
-    src = m.sample_sources(g, spec["S"], spec["seed"], min_degree=1)
+    if spec["kind"] == "batched":
+        return run_reference_batched(args, spec, m, oracle)
+    if spec["kind"] == "served":
+        g = make_graph(m, spec["graph"])
+        src = np.concatenate(make_requests(g, spec["requests"], spec["seed"]))
+    else:
+        g = make_graph(m, spec)
+        src = m.sample_sources(g, spec["S"], spec["seed"], min_degree=1)
     threads = os.cpu_count() or 1
     # calibrate a per-step sample of about 2 s
     t0 = time.perf_counter()
@@ -197,8 +217,10 @@ def run_reference(args, spec):
     tot = sum(times)
     value = n * args.steps / tot
     cfg = workload_config(args.workload, spec, g)
+    metric = ("served MS-BFS sources/sec (Poisson request stream, per-source stats)"
+              if spec["kind"] == "served" else "MS-BFS sources/sec")
     out = {
-        "metric": "MS-BFS sources/sec", "value": value, "unit": "sources/s",
+        "metric": metric, "value": value, "unit": "sources/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -206,6 +228,45 @@ def run_reference(args, spec):
         "cpu_baseline": {"value": value, "unit": "sources/s", "cores": threads, "kind": "port",
                          "sample": f"{n} of the {len(src)} sources per step, threaded FIFO "
                                    f"(cpu_bfs rayon_ms.rs restated in C)"},
+        "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_batched(args, spec, m, oracle):
+    """CPU reference arm of the batched configuration: the threaded FIFO
+    oracle over the graphs in order, each step a bounded sample (about 2 s)."""
+    items = make_batch(m, spec)
+    threads = os.cpu_count() or 1
+
+    def one_step(start):
+        n_src, t0, i = 0, time.perf_counter(), start
+        while time.perf_counter() - t0 < 2.0:
+            g, s = items[i % len(items)]
+            oracle.ms_bfs_threaded(g.num_vertices, g.row_offsets, g.col_indices, s, threads)
+            n_src += int(s.size)
+            i += 1
+        return n_src, time.perf_counter() - t0, i
+
+    pos = 0
+    for _ in range(args.warmup):
+        _, _, pos = one_step(pos)
+    tot_src, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, dt, pos = one_step(pos)
+        tot_src += n
+        tot_t += dt
+    value = tot_src / tot_t
+    out = {
+        "metric": "batched MS-BFS sources/sec (1,000 graphs, one launch)", "value": value,
+        "unit": "sources/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": args.workload, "graphs": len(items)},
+        "cpu_baseline": {"value": value, "unit": "sources/s", "cores": threads, "kind": "port",
+                         "sample": f"graphs in order for about 2 s per step ({tot_src} sources "
+                                   f"in {args.steps} steps), threaded FIFO per graph"},
         "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -453,6 +514,183 @@ def run_batched(args, spec):
     b.close()
 
 
+def make_requests(g, n, seed):
+    """Request stream of the served configuration: |S| uniform over
+    SERVED_SIZES (log-spaced), each a set of distinct sources drawn uniformly
+    among vertices of degree >= 1, sorted ascending."""
+    rng = np.random.default_rng(seed)
+    cand = np.flatnonzero(np.diff(g.row_offsets.astype(np.int64)) >= 1).astype(np.uint32)
+    reqs = []
+    for _ in range(n):
+        S = int(SERVED_SIZES[int(rng.integers(0, len(SERVED_SIZES)))])
+        pick = np.unique(cand[rng.integers(0, cand.size, 2 * S + 8)])
+        while pick.size < S:
+            pick = np.unique(np.concatenate([pick, cand[rng.integers(0, cand.size, S)]]))
+        reqs.append(np.sort(rng.permutation(pick)[:S]).astype(np.uint32))
+    return reqs
+
+
+def poisson_arrivals(n, rate_req_s, seed):
+    """Arrival offsets (s) of a Poisson stream; rate None = all at t=0."""
+    if rate_req_s is None:
+        return np.zeros(n)
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate_req_s, n))
+
+
+def _latency_summary(lat_ms, sizes):
+    lat = np.asarray(lat_ms)
+    small = lat[np.asarray(sizes) <= 64]
+    pct = lambda a, q: float(np.percentile(a, q)) if a.size else None  # noqa: E731
+    return {"p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "small_p50_ms": pct(small, 50),
+            "small_p99_ms": pct(small, 99), "small_requests": int(small.size)}
+
+
+def serve_stream(srv, reqs, arrivals):
+    """Submits each request at its arrival time from one thread and collects
+    results in another; returns outputs, latencies (ms from submission to
+    result in host memory) and the makespan (s, first arrival to last result)."""
+    import queue as _queue
+    n = len(reqs)
+    q = _queue.Queue()
+    t0 = time.perf_counter()
+
+    def submitter():
+        for i in range(n):
+            dt = t0 + arrivals[i] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ts = time.perf_counter()
+            q.put((i, srv.submit(reqs[i], srv.STATS), ts))
+
+    th = threading.Thread(target=submitter, daemon=True)
+    th.start()
+    outs, lat, done = [None] * n, [0.0] * n, [0.0] * n
+    for _ in range(n):
+        i, ticket, ts = q.get()
+        out, info = srv.wait(ticket)
+        if info["status"] != 0:
+            raise RuntimeError(f"request {i} failed with status {info['status']}")
+        outs[i] = out
+        lat[i] = info["latency_ms"] + 1000.0 * (ts - (t0 + arrivals[i])) * (ts > t0 + arrivals[i])
+        done[i] = ts + info["latency_ms"] / 1000.0
+    th.join()
+    return outs, lat, max(done) - (t0 + arrivals[0])
+
+
+def plain_stream(eng, g, reqs, arrivals):
+    """The plain path: one engine call per request, one request at a time,
+    in arrival order (a FIFO queue in front of a single blocking call)."""
+    n = len(reqs)
+    outs, lat = [None] * n, [0.0] * n
+    t0 = time.perf_counter()
+    t_end = t0
+    for i in range(n):
+        dt = t0 + arrivals[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        outs[i] = eng.run_ms_bfs_stats(g, reqs[i])
+        t_end = time.perf_counter()
+        lat[i] = 1000.0 * (t_end - (t0 + arrivals[i]))
+    return outs, lat, t_end - (t0 + arrivals[0])
+
+
+def served_experiment(m, g, reqs, cfg, fractions=(0.3, 0.6, 0.9), seed=0, warm=40):
+    """Capacity (all requests at t=0) of the served form and of the plain
+    path, then Poisson streams offered at fractions of the served capacity
+    through both. Every served result is compared with the plain one."""
+    import torch
+    sizes = [int(r.size) for r in reqs]
+    total = float(sum(sizes))
+    eng = m.GpuBfsEngine(m.GpuBfsMethod.Auto)
+    eng.set_stream(torch.cuda.Stream().cuda_stream)
+    srv = m.BfsServer(g, **cfg)
+    try:
+        for r in reqs[:warm]:  # first use of each lane width builds its workspace
+            eng.run_ms_bfs_stats(g, r)
+        serve_stream(srv, reqs[:warm], np.zeros(min(warm, len(reqs))))
+        c0 = srv.counters()
+        with ClockSampler(0) as clk:
+            s_out, s_lat, s_span = serve_stream(srv, reqs, np.zeros(len(reqs)))
+        c1 = srv.counters()
+        p_out, p_lat, p_span = plain_stream(eng, g, reqs, np.zeros(len(reqs)))
+        same = sum(a.tobytes() == b.tobytes() for a, b in zip(s_out, p_out))
+        cap_s, cap_p = total / s_span, total / p_span
+        sweep = []
+        for k, f in enumerate(fractions):
+            rate = f * cap_s / (total / len(reqs))  # requests/s
+            arr = poisson_arrivals(len(reqs), rate, seed + k)
+            so, sl, ss = serve_stream(srv, reqs, arr)
+            po, pl, ps = plain_stream(eng, g, reqs, arr)
+            same += sum(a.tobytes() == b.tobytes() for a, b in zip(so, po))
+            sweep.append({"offered_sources_per_s": f * cap_s, "offered_fraction": f,
+                          "served": dict(_latency_summary(sl, sizes),
+                                         sources_per_s=total / ss),
+                          "plain": dict(_latency_summary(pl, sizes), sources_per_s=total / ps)})
+        return {
+            "served_capacity": cap_s, "plain_capacity": cap_p,
+            "served_saturated": dict(_latency_summary(s_lat, sizes), makespan_s=s_span),
+            "plain_saturated": dict(_latency_summary(p_lat, sizes), makespan_s=p_span),
+            "sweep": sweep, "identical_results": same,
+            "compared_results": len(reqs) * (1 + len(fractions)),
+            "traversals": c1["traversals"] - c0["traversals"],
+            "kernel_launches": c1["kernel_launches"] - c0["kernel_launches"],
+            "clocks": clk.summary(),
+        }
+    finally:
+        srv.close()
+        eng.close()
+
+
+def run_served(args, spec):
+    """Served form vs the plain one-request-at-a-time path on a resident graph."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import webgpu_bfs_gb300 as m
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    gs = spec["graph"]
+    g = make_graph(m, gs)
+    gen_s = time.perf_counter() - t0
+    reqs = make_requests(g, spec["requests"], spec["seed"])
+    total = sum(int(r.size) for r in reqs)
+    r = served_experiment(m, g, reqs, SERVED_CONFIG, seed=spec["seed"])
+    ok = [p for p in r["sweep"] if p["served"]["small_p99_ms"] is not None
+          and p["served"]["small_p99_ms"] <= 20.0]
+    sat = r["served_saturated"]
+    res = {
+        "metric": "served MS-BFS sources/sec (Poisson request stream, per-source stats)",
+        "value": r["served_capacity"], "unit": "sources/s", "n_gpus": 1,
+        "steps": len(reqs), "warmup": 40, "ms_per_step": 1000.0 * sat["makespan_s"] / len(reqs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "graph": gs, "num_vertices": g.num_vertices,
+                   "num_edges": g.num_edges, "requests": len(reqs), "sources": total,
+                   "request_sizes": list(SERVED_SIZES), "server": SERVED_CONFIG,
+                   "output": "per-source eccentricity, reached count, distance sum",
+                   "generation_s": round(gen_s, 1),
+                   "l2_policy": "graph and traversal state larger than L2"},
+        "plain_one_request_per_launch": {"value": r["plain_capacity"], "unit": "sources/s",
+                                         **r["plain_saturated"]},
+        "speedup_vs_plain": r["served_capacity"] / r["plain_capacity"],
+        "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"],
+        "sweep": r["sweep"],
+        "best_sources_per_s_with_small_p99_le_20ms":
+            max((p["served"]["sources_per_s"] for p in ok), default=None),
+        "parity": f"{r['identical_results']}/{r['compared_results']} served results "
+                  f"identical to the plain path",
+        "e2e": {"value": r["served_capacity"], "unit": "sources/s",
+                "h2d_bytes_per_step": int(4 * total / len(reqs)),
+                "d2h_bytes_per_step": int(16 * total / len(reqs)),
+                "note": "the server API is host to host: sources in, statistics out"},
+        "clocks": r["clocks"],
+        "traversals": r["traversals"],
+        "gpu_launches": r["kernel_launches"],
+    }
+    print(json.dumps(res), flush=True)
+
+
 def run_ncu_case(args, spec):
     """A single small invocation for ncu captures (few GB on the device)."""
     os.environ["MSBFS_HOST_LOOP"] = "1"
@@ -495,6 +733,8 @@ def main():
         run_ncu_case(args, spec)
     elif spec["kind"] == "batched" and args.impl != "reference":
         run_batched(args, spec)
+    elif spec["kind"] == "served" and args.impl != "reference":
+        run_served(args, spec)
     elif args.impl == "reference":
         run_reference(args, spec)
     else:

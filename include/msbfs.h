@@ -47,6 +47,8 @@ extern "C" {
 #define MSBFS_ERR_NO_DEVICE 8
 /* The graph does not fit the fixed scratch of msbfs_run_cta_noalloc. */
 #define MSBFS_ERR_SCRATCH_TOO_SMALL 9
+/* A Matrix Market file was rejected (details in msbfs_mtx_error). */
+#define MSBFS_ERR_PARSE 10
 
 /* ---- methods: same names and order as GpuBfsMethod (engine.rs:33-53) ------
  * Every method produces identical bytes. On GB300 they map onto four kernel
@@ -148,6 +150,11 @@ int msbfs_engine_set_stream(msbfs_engine *engine, void *cuda_stream);
  * chunks in multi_word_bp.rs:630). Zero keeps the current value. */
 int msbfs_engine_set_tuning(msbfs_engine *engine, uint32_t max_words_per_pass,
                             uint32_t alpha, uint32_t beta);
+/* Caps the persistent kernels' grids at `percent` (1..100, default 100) of
+ * the blocks that fit the device at once, leaving the rest of the SMs to
+ * kernels of other streams (the served form gives them to its express
+ * slots). No reference counterpart. Results do not depend on it. */
+int msbfs_engine_set_sm_share(msbfs_engine *engine, uint32_t percent);
 
 /* Profiling: 0 off; 1 keep a per-level record of every call (device timers,
  * the level loop stays on the device); 2 as 1, but the level loop is driven
@@ -243,7 +250,15 @@ int msbfs_run_ms_bfs_stats(msbfs_engine *engine, const msbfs_graph *graph,
  * traversal state is allocated once, and distance rows are staged in at most
  * hbm_budget_bytes / slots per slot, so a request needing more rows than a
  * slot can stage is split across launches. Every result is the same bytes
- * as a lone msbfs_run_ms_bfs / msbfs_run_ms_bfs_stats call. */
+ * as a lone msbfs_run_ms_bfs / msbfs_run_ms_bfs_stats call.
+ *
+ * Latency: a request of at most small_sources sources is "small". The first
+ * express_slots slots take only small requests (at most 2*small_sources
+ * lanes per launch, so their traversals stay narrow) on the device's
+ * highest-priority streams; the other slots take large requests first, in
+ * arrival order, and small ones only when no large request waits. Their
+ * persistent kernels use general_sm_percent of the resident grid
+ * (msbfs_engine_set_sm_share) so express kernels find SMs free. */
 #define MSBFS_SERVE_ROWS 0  /* out = S*V u32 distance rows          */
 #define MSBFS_SERVE_STATS 1 /* out = S msbfs_source_stats           */
 typedef struct msbfs_server msbfs_server;
@@ -252,7 +267,15 @@ typedef struct msbfs_server_config {
   uint32_t max_sources_per_launch; /* lanes packed per launch (0 -> 512)       */
   uint64_t hbm_budget_bytes;       /* row staging, all slots (0 -> 8 GiB)      */
   int method;                      /* engine method (MSBFS_METHOD_AUTO)        */
+  uint32_t express_slots;          /* slots reserved for small requests (0)    */
+  uint32_t small_sources;          /* small-request threshold (0 -> 64)        */
+  uint32_t general_sm_percent;     /* grid share of the other slots (0 -> 100) */
+  uint32_t reserved;               /* must be 0                                */
 } msbfs_server_config;
+/* Totals since creation: traversals launched and kernel launches (level
+ * loop launches counted from each traversal's level count). */
+int msbfs_server_counters(msbfs_server *server, uint64_t *traversals,
+                          uint64_t *kernel_launches);
 typedef struct msbfs_request_info {
   double latency_ms; /* submit -> result in host memory       */
   double queue_ms;   /* submit -> first launch                */
@@ -342,6 +365,31 @@ int msbfs_csr_to_undirected(const msbfs_csr *in, msbfs_csr *out);
 int msbfs_csr_validate(const msbfs_csr *csr, char *msg, size_t msg_len);
 /* CsrGraph::max_degree (graph.rs:209-214). */
 uint32_t msbfs_csr_max_degree(const msbfs_csr *csr);
+
+/* ==================== Matrix Market reader (crates/core/src/mtx.rs) ========
+ * MtxReader::parse (mtx.rs:124-275): coordinate format only; pattern, real,
+ * integer or complex fields (values ignored); symmetric, skew-symmetric and
+ * hermitian matrices must be square and are expanded to both directions;
+ * 1-based indices; self-loops dropped; V = max(rows, cols); adjacency sorted
+ * and deduplicated. On MSBFS_ERR_PARSE, `err` (optional) holds the MtxError
+ * variant (crates/core/src/error.rs:43-81), its fields and its message. */
+#define MSBFS_MTX_OK 0
+#define MSBFS_MTX_IO 1
+#define MSBFS_MTX_INVALID_HEADER 2
+#define MSBFS_MTX_UNSUPPORTED_FORMAT 3
+#define MSBFS_MTX_INVALID_DIMENSIONS 4
+#define MSBFS_MTX_INVALID_COORDINATE_LINE 5
+#define MSBFS_MTX_ZERO_INDEX 6
+#define MSBFS_MTX_INDEX_OUT_OF_BOUNDS 7
+typedef struct msbfs_mtx_error {
+  int kind;              /* MSBFS_MTX_*                                  */
+  uint64_t line_number;  /* 1-based line of the offending text (0: none) */
+  uint64_t row, col;     /* ZERO_INDEX / INDEX_OUT_OF_BOUNDS entry        */
+  uint64_t max_rows, max_cols;
+  char message[256];     /* the reference's error text                   */
+} msbfs_mtx_error;
+int msbfs_mtx_parse(const char *text, size_t len, msbfs_csr *out, msbfs_mtx_error *err);
+int msbfs_mtx_read(const char *path, msbfs_csr *out, msbfs_mtx_error *err);
 
 /* ==================== generators (crates/core/src/generators.rs) ==========
  * Seeded with the engine's own counter-based generator (splitmix64), so the

@@ -212,3 +212,26 @@ def test_page_locked_host_output(native, oracle):
             assert_same(out, _oracle(oracle, g, src), g, src, f"pinned/V={g.num_vertices}")
     finally:
         eng.close()
+
+
+def test_cta_global_bitmap_beyond_shared_memory(native, oracle):
+    """Road graph whose visited bitmap exceeds shared memory (1,960,000
+    vertices > 8 bits x 227 KB): the CTA path keeps its bitmap in an
+    L2-resident global slab per block. Rows, statistics and the queue slab
+    that alternates ends by level are checked over thousands of levels."""
+    g = native.wilson_grid(1400, 1400, 2000, 11)
+    src = native.sample_sources(g, 20, 4)
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.WorkgroupPersistentBfs)
+    try:
+        got = eng.run_ms_bfs(g, src)
+        assert eng.last_stats["path"] == 4  # CTA path, not the level-path fallback
+        want = _oracle(oracle, g, src)
+        assert_same(got, want, g, src, "global-bitmap CTA rows")
+        st = eng.run_ms_bfs_stats(g, src)
+        d = want.reshape(len(src), g.num_vertices).astype(np.int64)
+        fin = d != 0xFFFFFFFF
+        assert np.array_equal(st["reached"], fin.sum(1))
+        assert np.array_equal(st["eccentricity"], np.where(fin, d, 0).max(1))
+        assert np.array_equal(st["distance_sum"], np.where(fin, d, 0).sum(1))
+    finally:
+        eng.close()

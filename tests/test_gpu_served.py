@@ -60,18 +60,22 @@ def _requests(rng, V, n):
     return out
 
 
-@pytest.mark.parametrize("graph_kind", ["rmat", "road"])
-def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind):
+@pytest.mark.parametrize("graph_kind,express", [("rmat", 0), ("road", 0), ("rmat", 1),
+                                                ("road", 1)])
+def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind, express):
     torch = pytest.importorskip("torch")
     if graph_kind == "rmat":
         g = native.generate_graph500_rmat(12, 8, 71)
     else:
         g = native.wilson_grid(60, 60, 72, 8)
     V = g.num_vertices
-    rng = np.random.default_rng(3)
+    rng = np.random.default_rng(3 + express)
     reqs = _requests(rng, V, 14)
-    srv = native.BfsServer(g, slots=2, max_sources_per_launch=512,
-                           hbm_budget_bytes=2 * 300 * V * 4)  # forces row splitting
+    slots = 2 + express
+    srv = native.BfsServer(g, slots=slots, max_sources_per_launch=512,
+                           hbm_budget_bytes=slots * 300 * V * 4,  # forces row splitting
+                           express_slots=express, small_sources=8,
+                           general_sm_percent=70 if express else 100)
     try:
         # in the mix: submitted from two threads, interleaved
         tickets = [None] * len(reqs)
@@ -106,8 +110,38 @@ def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind):
             else:
                 assert res.tobytes() == mixed[i].tobytes(), f"request {i} stats alone vs mix"
                 _same_stats(res, _oracle_stats(oracle, g, src), f"request {i} stats")
+        c = srv.counters()
+        assert c["traversals"] >= 1 and c["kernel_launches"] >= c["traversals"]
     finally:
         srv.close()
+
+
+def test_server_config_rejected(native):
+    g = native.generate_graph500_rmat(8, 8, 5)
+    with pytest.raises(native.BfsError):
+        native.BfsServer(g, slots=2, express_slots=2)  # no general slot left
+    with pytest.raises(native.BfsError):
+        native.BfsServer(g, slots=2, general_sm_percent=101)
+
+
+def test_sm_share_same_results(native, oracle):
+    g = native.generate_graph500_rmat(12, 16, 77)
+    src = native.sample_sources(g, 300, 5, min_degree=1)
+    eng = native.GpuBfsEngine()
+    try:
+        full = eng.run_ms_bfs(g, src)
+        for pct in (1, 37):
+            eng.set_sm_share(pct)
+            assert_same(eng.run_ms_bfs(g, src), full, g, src, f"sm share {pct}%")
+        with pytest.raises(native.BfsError):
+            eng.set_sm_share(0)
+        road = native.wilson_grid(40, 40, 30, 3)  # CTA path
+        rs = native.sample_sources(road, 50, 1)
+        assert_same(eng.run_ms_bfs(road, rs),
+                    oracle.ms_bfs_fifo(road.num_vertices, road.row_offsets, road.col_indices,
+                                       rs), road, rs, "CTA path, sm share 37%")
+    finally:
+        eng.close()
 
 
 def test_server_wait_timeout_and_empty(native):

@@ -32,14 +32,16 @@ __all__ = [
     "generate_random_tree", "generate_rmat", "generate_graph500_rmat", "empty_graph",
     "isolated_vertices", "single_vertex", "path_graph", "star_graph", "cycle_graph",
     "clique_graph", "disconnected_cliques", "wilson_grid", "sample_sources",
-    "GRAPH500_A", "GRAPH500_B", "GRAPH500_C", "GRAPH500_D",
+    "GRAPH500_A", "GRAPH500_B", "GRAPH500_C", "GRAPH500_D", "BfsServer", "BatchedBfs",
+    "MtxError", "parse_mtx", "read_mtx", "SOURCE_STATS_DTYPE",
 ]
 
 UNREACHABLE = 0xFFFFFFFF
 
 ERROR_NAMES = {
     1: "SourceOutOfBounds", 2: "EmptyGraph", 3: "OutOfMemory", 4: "Timeout", 5: "Cuda",
-    6: "InvalidGraph", 7: "InvalidArgument", 8: "NoDevice",
+    6: "InvalidGraph", 7: "InvalidArgument", 8: "NoDevice", 9: "ScratchTooSmall",
+    10: "Parse",
 }
 
 
@@ -511,27 +513,28 @@ class GpuBfsEngine:
             self._h, dg.handle, C.c_void_p(dist_ptr), num_sources, C.byref(out)))
         return out.value
 
+    def run_ms_bfs_stats(self, graph: CsrGraph, sources) -> np.ndarray:
+        """Per-source eccentricity / reached count / distance sum, computed on
+        the device without forming the S*V matrix (msbfs_run_ms_bfs_stats)."""
+        src = _u32(sources)
+        out = np.zeros(src.size, SOURCE_STATS_DTYPE)
+        if src.size == 0:
+            return out
+        dg = self.upload(graph)
+        st = Stats()
+        rc = _native.lib().msbfs_run_ms_bfs_stats(self._h, dg.handle, _ptr(src), src.size,
+                                                  out.ctypes.data_as(C.c_void_p), C.byref(st))
+        self._check(rc)
+        self.last_stats = st.as_dict()
+        return out
+
+    def set_sm_share(self, percent: int) -> None:
+        """Caps the persistent kernels' grids at ``percent`` of the resident
+        capacity (msbfs_engine_set_sm_share)."""
+        self._check(_native.lib().msbfs_engine_set_sm_share(self._h, int(percent)))
+
 
 SOURCE_STATS_DTYPE = np.dtype(_native.SOURCE_STATS_DTYPE)
-
-
-def _engine_run_ms_bfs_stats(self, graph: "CsrGraph", sources) -> np.ndarray:
-    """Per-source eccentricity / reached count / distance sum, computed on the
-    device without forming the S*V matrix (msbfs_run_ms_bfs_stats)."""
-    src = _u32(sources)
-    out = np.zeros(src.size, SOURCE_STATS_DTYPE)
-    if src.size == 0:
-        return out
-    dg = self.upload(graph)
-    st = Stats()
-    rc = _native.lib().msbfs_run_ms_bfs_stats(self._h, dg.handle, _ptr(src), src.size,
-                                              out.ctypes.data_as(C.c_void_p), C.byref(st))
-    self._check(rc)
-    self.last_stats = st.as_dict()
-    return out
-
-
-GpuBfsEngine.run_ms_bfs_stats = _engine_run_ms_bfs_stats
 
 
 class ServerTicket:
@@ -552,8 +555,10 @@ class BfsServer:
 
     def __init__(self, graph: "CsrGraph", slots: int = 2, max_sources_per_launch: int = 512,
                  hbm_budget_bytes: int = 0, method: GpuBfsMethod = GpuBfsMethod.Auto,
-                 device: int = 0):
-        cfg = _native.ServerConfig(slots, max_sources_per_launch, hbm_budget_bytes, int(method))
+                 device: int = 0, express_slots: int = 0, small_sources: int = 64,
+                 general_sm_percent: int = 100):
+        cfg = _native.ServerConfig(slots, max_sources_per_launch, hbm_budget_bytes, int(method),
+                                   express_slots, small_sources, general_sm_percent, 0)
         h = C.c_void_p()
         self.graph = graph
         self.V = graph.num_vertices
@@ -580,6 +585,13 @@ class BfsServer:
                                              C.byref(info))
         _check(rc, "request failed")
         return ticket.out, info.as_dict()
+
+    def counters(self) -> dict:
+        """Traversals and kernel launches issued since creation."""
+        t, k = C.c_uint64(), C.c_uint64()
+        _check(_native.lib().msbfs_server_counters(self._h, C.byref(t), C.byref(k)),
+               "counters failed")
+        return {"traversals": t.value, "kernel_launches": k.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -778,3 +790,41 @@ def sample_sources(graph: CsrGraph, count: int, seed: int, min_degree: int = 0) 
                                             seed & (2**64 - 1), min_degree, _ptr(out))
     _check(rc, "not enough eligible vertices")
     return out
+
+
+class MtxError(BfsError):
+    """MtxError of the reference (crates/core/src/error.rs:43-81): ``kind`` is
+    the variant name, the other attributes its fields (0 when unused)."""
+
+    KINDS = {1: "Io", 2: "InvalidHeader", 3: "UnsupportedFormat", 4: "InvalidDimensions",
+             5: "InvalidCoordinateLine", 6: "ZeroIndex", 7: "IndexOutOfBounds"}
+
+    def __init__(self, err: "_native.MtxErrorInfo"):
+        super().__init__(10, err.message.decode(errors="replace"))
+        self.kind = self.KINDS.get(err.kind, f"kind {err.kind}")
+        self.line_number = err.line_number
+        self.row, self.col = err.row, err.col
+        self.max_rows, self.max_cols = err.max_rows, err.max_cols
+
+
+def _mtx_result(rc: int, c: Csr, err) -> CsrGraph:
+    if rc == 10:
+        raise MtxError(err)
+    _check(rc, "Matrix Market read failed")
+    V, _, off, idx = _take_csr(c)
+    return CsrGraph(V, off, idx)
+
+
+def parse_mtx(text) -> CsrGraph:
+    """MtxReader::parse (crates/core/src/mtx.rs:124) of Matrix Market text."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    c, err = Csr(), _native.MtxErrorInfo()
+    rc = _native.lib().msbfs_mtx_parse(data, len(data), C.byref(c), C.byref(err))
+    return _mtx_result(rc, c, err)
+
+
+def read_mtx(path) -> CsrGraph:
+    """Reads a Matrix Market (.mtx) file into a CsrGraph."""
+    c, err = Csr(), _native.MtxErrorInfo()
+    rc = _native.lib().msbfs_mtx_read(str(path).encode(), C.byref(c), C.byref(err))
+    return _mtx_result(rc, c, err)

@@ -73,6 +73,10 @@ class ServerConfig(C.Structure):
         ("max_sources_per_launch", C.c_uint32),
         ("hbm_budget_bytes", C.c_uint64),
         ("method", C.c_int),
+        ("express_slots", C.c_uint32),
+        ("small_sources", C.c_uint32),
+        ("general_sm_percent", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -86,6 +90,18 @@ class RequestInfo(C.Structure):
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class MtxErrorInfo(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("line_number", C.c_uint64),
+        ("row", C.c_uint64),
+        ("col", C.c_uint64),
+        ("max_rows", C.c_uint64),
+        ("max_cols", C.c_uint64),
+        ("message", C.c_char * 256),
+    ]
 
 
 # numpy view of msbfs_source_stats
@@ -111,6 +127,7 @@ SIGNATURES = {
     "msbfs_engine_last_error": (C.c_char_p, [C.c_void_p]),
     "msbfs_engine_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "msbfs_engine_set_tuning": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "msbfs_engine_set_sm_share": (C.c_int, [C.c_void_p, C.c_uint32]),
     "msbfs_engine_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "msbfs_engine_level_log": (C.c_int, [C.c_void_p, C.POINTER(LevelRecord), C.c_size_t,
                                          sizep]),
@@ -144,6 +161,7 @@ SIGNATURES = {
                                       C.POINTER(C.c_uint64)]),
     "msbfs_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double,
                                     C.POINTER(RequestInfo)]),
+    "msbfs_server_counters": (C.c_int, [C.c_void_p, u64p, u64p]),
     "msbfs_server_destroy": (None, [C.c_void_p]),
     "msbfs_batch_create": (C.c_int, [C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
     "msbfs_batch_destroy": (None, [C.c_void_p]),
@@ -161,6 +179,9 @@ SIGNATURES = {
     "msbfs_csr_to_undirected": (C.c_int, [C.POINTER(Csr), C.POINTER(Csr)]),
     "msbfs_csr_validate": (C.c_int, [C.POINTER(Csr), C.c_char_p, C.c_size_t]),
     "msbfs_csr_max_degree": (C.c_uint32, [C.POINTER(Csr)]),
+    "msbfs_mtx_parse": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(Csr),
+                                  C.POINTER(MtxErrorInfo)]),
+    "msbfs_mtx_read": (C.c_int, [C.c_char_p, C.POINTER(Csr), C.POINTER(MtxErrorInfo)]),
     "msbfs_gen_grid2d": (C.c_int, [C.c_size_t, C.c_size_t, C.POINTER(Csr)]),
     "msbfs_gen_erdos_renyi_np": (C.c_int, [C.c_size_t, C.c_double, C.c_uint64,
                                            C.POINTER(Csr)]),

@@ -6,11 +6,13 @@
 // reference: one workgroup runs a whole single-source BFS with its visited
 // bitmap in shared memory and synchronises only inside the block, so a
 // ~1,000-level traversal needs no grid-wide step. The GB300 form differs:
-// the bitmap takes up to ~200 KB of shared memory (vs 14 KB), the frontier
-// queues live in an L2-resident global slab per resident block (no overflow
-// fallback), distances are exact u32 written into the caller's row, and the
-// grid is persistent: each resident block pulls the next source from an
-// atomic cursor until all sources are done. No block ever waits on another.
+// the bitmap takes up to ~227 KB of shared memory (vs 14 KB) and, for larger
+// graphs, moves to an L2-resident global slab per block instead of giving up
+// the path; the frontier queues live in one L2-resident global slab of V
+// words per resident block (no overflow fallback), distances are exact u32
+// written into the caller's row, and the grid is persistent: each resident
+// block pulls the next source from an atomic cursor until all sources are
+// done. No block ever waits on another.
 #include <algorithm>
 #include <mutex>
 
@@ -20,80 +22,94 @@
 namespace msbfs {
 
 constexpr uint32_t CTA_DIST_MAX = 0xffffffffu;
+constexpr int CTA_THREADS = 512;
+// Global-bitmap mode keeps its per-block scratch (queue slab + bitmap) within
+// this many bytes by shrinking the grid.
+constexpr size_t CTA_GLOBAL_SCRATCH_BYTES = 4ull << 30;
 
-__global__ void cta_bfs_kernel(CtaParams p) {
-  extern __shared__ uint32_t bitmap[];
+// GB: the visited bitmap lives in an L2-resident global slab per block (for
+// graphs whose bitmap does not fit shared memory) instead of shared memory.
+//
+// Queue: one slab of V words per block. The frontiers of consecutive levels
+// are disjoint vertex sets, so |F_L| + |F_L+1| <= V: even levels read from
+// the front of the slab and append at the back, odd levels the reverse.
+// Counters: level L appends through s_cnt[L % 3]; thread 0 clears
+// s_cnt[(L+1) % 3] during level L (last read right after the barrier of
+// level L-2), so a level needs one block barrier.
+template <bool GB>
+__global__ void __launch_bounds__(CTA_THREADS) cta_bfs_kernel(CtaParams p) {
+  extern __shared__ uint32_t smem_bits[];
   __shared__ uint32_t s_src_idx;
-  __shared__ uint32_t s_count;
+  __shared__ uint32_t s_cnt[3];
   __shared__ unsigned long long s_sum;
   __shared__ uint32_t s_reached;
   const uint32_t V = p.V;
   const uint32_t words = (V + 31) / 32;
-  uint32_t* qa = p.gqueue + (size_t)blockIdx.x * 2 * V;
-  uint32_t* qb = qa + V;
+  uint32_t* bits = GB ? p.gbits + (size_t)blockIdx.x * words : smem_bits;
+  uint32_t* slab = p.gqueue + (size_t)blockIdx.x * V;
 
   for (;;) {
     if (threadIdx.x == 0) {
       s_src_idx = atomicAdd(p.work, 1u);
       s_sum = 0;
       s_reached = 0;
+      s_cnt[0] = s_cnt[1] = s_cnt[2] = 0;
     }
-    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) bitmap[i] = 0;
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) bits[i] = 0;
     __syncthreads();
     const uint32_t si = s_src_idx;
     if (si >= p.num_sources) break;
     const uint32_t src = p.sources[si];
     uint32_t* row = p.dist ? p.dist + (size_t)si * V : nullptr;
     if (threadIdx.x == 0) {
-      bitmap[src >> 5] = 1u << (src & 31);
+      bits[src >> 5] = 1u << (src & 31);
       if (row) row[src] = 0;
-      qa[0] = src;
-      s_count = 0;
+      slab[0] = src;
     }
     uint32_t n_in = 1;
     uint32_t level = 0, ecc = 0;
     unsigned long long my_sum = 0;
     uint32_t my_cnt = 0;
-    uint32_t* qin = qa;
-    uint32_t* qout = qb;
     __syncthreads();
     while (n_in) {
       ecc = level;
       const uint32_t nd = level + 1;
+      const bool front = (level & 1) == 0;  // where this level's frontier sits
+      uint32_t* cnt = &s_cnt[level % 3];
+      if (threadIdx.x == 0) s_cnt[(level + 1) % 3] = 0;
       // Threads sweep the frontier; each expands one vertex's out-edges.
-      const uint32_t n_round = (n_in + blockDim.x - 1) / blockDim.x * blockDim.x;
-      for (uint32_t i = threadIdx.x; i < n_round; i += blockDim.x) {
-        if (i < n_in) {
-          const uint32_t u = qin[i];
-          const uint32_t eb = __ldg(p.off + u), ee = __ldg(p.off + u + 1);
-          for (uint32_t e = eb; e < ee; ++e) {
-            const uint32_t v = __ldg(p.idx + e);
-            const uint32_t bit = 1u << (v & 31);
-            if (bitmap[v >> 5] & bit) continue;
-            const uint32_t old = atomicOr(&bitmap[v >> 5], bit);
-            if (old & bit) continue;
-            if (row) row[v] = nd;
-            my_sum += nd;
-            ++my_cnt;
-            const uint32_t pos = atomicAdd(&s_count, 1u);
-            qout[pos] = v;
+      for (uint32_t i = threadIdx.x; i < n_in; i += blockDim.x) {
+        const uint32_t u = front ? slab[i] : slab[V - 1 - i];
+        const uint32_t eb = __ldg(p.off + u), ee = __ldg(p.off + u + 1);
+        for (uint32_t e = eb; e < ee; ++e) {
+          const uint32_t v = __ldg(p.idx + e);
+          const uint32_t bit = 1u << (v & 31);
+          if constexpr (!GB) {
+            if (bits[v >> 5] & bit) continue;
           }
+          const uint32_t old = atomicOr(&bits[v >> 5], bit);
+          if (old & bit) continue;
+          if (row) row[v] = nd;
+          my_sum += nd;
+          ++my_cnt;
+          const uint32_t pos = atomicAdd(cnt, 1u);
+          if (front)
+            slab[V - 1 - pos] = v;
+          else
+            slab[pos] = v;
         }
       }
       __syncthreads();
-      n_in = s_count;
-      __syncthreads();
-      if (threadIdx.x == 0) s_count = 0;
-      uint32_t* t = qin;
-      qin = qout;
-      qout = t;
+      n_in = *cnt;
       ++level;
-      __syncthreads();
     }
     if (row) {
-      // Unreached vertices: coalesced sweep of the row guided by the bitmap.
-      for (uint32_t v = threadIdx.x; v < V; v += blockDim.x)
-        if (!((bitmap[v >> 5] >> (v & 31)) & 1u)) row[v] = CTA_DIST_MAX;
+      // Unreached vertices: coalesced sweep of the row guided by the bitmap
+      // (read from L2 in global mode: the bits were set by atomics).
+      for (uint32_t v = threadIdx.x; v < V; v += blockDim.x) {
+        const uint32_t w = GB ? __ldcg(bits + (v >> 5)) : bits[v >> 5];
+        if (!((w >> (v & 31)) & 1u)) row[v] = CTA_DIST_MAX;
+      }
     }
     if (p.stats) {
       if (my_cnt) {
@@ -119,31 +135,46 @@ size_t cta_max_vertices(int device) {
   return ((size_t)optin - reserve) * 8;
 }
 
-bool cta_launch_shape(uint32_t V, int device, int* grid, int* block, size_t* smem) {
-  if ((size_t)V > cta_max_vertices(device)) return false;
-  const size_t bytes = ((size_t)V + 31) / 32 * sizeof(uint32_t);
-  const int threads = 256;
-  cudaFuncSetAttribute(cta_bfs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel, threads, bytes);
-  if (occ < 1) return false;
+bool cta_launch_shape(uint32_t V, int device, bool allow_global, CtaShape* out) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  *grid = sms * occ;
-  *block = threads;
-  *smem = bytes;
+  const size_t words = ((size_t)V + 31) / 32;
+  CtaShape sh{};
+  sh.block = CTA_THREADS;
+  int occ = 0;
+  if ((size_t)V <= cta_max_vertices(device)) {
+    sh.smem = words * sizeof(uint32_t);
+    cudaFuncSetAttribute(cta_bfs_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sh.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<false>, sh.block,
+                                                  sh.smem);
+    if (occ < 1) return false;
+    sh.grid = sms * occ;
+  } else {
+    if (!allow_global) return false;
+    sh.global_bits = true;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<true>, sh.block, 0);
+    if (occ < 1) return false;
+    const size_t per_block = ((size_t)V + words) * sizeof(uint32_t);
+    sh.grid = (int)std::max<size_t>(
+        1, std::min<size_t>((size_t)sms * occ, CTA_GLOBAL_SCRATCH_BYTES / per_block));
+  }
+  *out = sh;
   return true;
 }
 
-void launch_cta(const CtaParams& p, int grid, int block, size_t smem, cudaStream_t s) {
-  cta_bfs_kernel<<<grid, block, smem, s>>>(p);
+void launch_cta(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s) {
+  if (sh.global_bits)
+    cta_bfs_kernel<true><<<grid, sh.block, 0, s>>>(p);
+  else
+    cta_bfs_kernel<false><<<grid, sh.block, sh.smem, s>>>(p);
 }
 
 // ---------------------------------------------------------------------------
 // Allocation-free form of the CTA-per-source launch.
 //
 // Its scratch -- a copy of the sources, the source cursor and one frontier
-// queue slab (2*V words) per resident block -- lives in this fixed array
+// queue slab (V words) per resident block -- lives in this fixed array
 // instead of engine-owned cudaMalloc memory, so the entry point below never
 // allocates. Every GPU that loads the library holds the array until exit.
 // Layout in u32 words: [0] source cursor, [NOALLOC_SRC_OFF, +NOALLOC_SRC_CAP)
@@ -177,7 +208,7 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
   // Size limits, checked before touching the device: the visited bitmap must
   // fit shared memory and at least one queue slab must fit the scratch array.
   if (num_vertices > MSBFS_NOALLOC_MAX_VERTICES ||
-      NOALLOC_Q_OFF + 2 * num_vertices > NOALLOC_WORDS)
+      NOALLOC_Q_OFF + num_vertices > NOALLOC_WORDS)
     return MSBFS_ERR_SCRATCH_TOO_SMALL;
   if (cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
@@ -200,10 +231,10 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
     base = g_noalloc_addr[device];
   }
   const uint32_t V = (uint32_t)num_vertices;
-  int grid = 0, block = 0;
-  size_t smem = 0;
-  if (!cta_launch_shape(V, device, &grid, &block, &smem)) return MSBFS_ERR_SCRATCH_TOO_SMALL;
-  const size_t slabs = (NOALLOC_WORDS - NOALLOC_Q_OFF) / (2 * (size_t)V);
+  CtaShape sh{};
+  if (!cta_launch_shape(V, device, /*allow_global=*/false, &sh))
+    return MSBFS_ERR_SCRATCH_TOO_SMALL;
+  const size_t slabs = (NOALLOC_WORDS - NOALLOC_Q_OFF) / (size_t)V;
   const cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   for (size_t s0 = 0; s0 < num_sources; s0 += NOALLOC_SRC_CAP) {
     const size_t n = std::min(NOALLOC_SRC_CAP, num_sources - s0);
@@ -223,8 +254,8 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
     cp.dist = dist_device + s0 * num_vertices;
     cp.gqueue = base + NOALLOC_Q_OFF;
     cp.work = base;
-    const int blocks = (int)std::min<size_t>({(size_t)grid, n, slabs});
-    launch_cta(cp, blocks, block, smem, s);
+    const int blocks = (int)std::min<size_t>({(size_t)sh.grid, n, slabs});
+    launch_cta(cp, sh, blocks, s);
     if (cudaGetLastError() != cudaSuccess) return MSBFS_ERR_CUDA;
   }
   return MSBFS_OK;

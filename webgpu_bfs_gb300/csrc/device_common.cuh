@@ -135,7 +135,7 @@ struct LevelParams {
   uint32_t* hcount;   // [n_heavy] slices finished this level
   uint32_t bits_div;  // bitmap check when the frontier holds < V / bits_div vertices
   uint32_t n_order;
-  const uint32_t* order;  // vertices with 0 < in-degree <= split, in-degree descending
+  const uint32_t* order;  // vertices with 0 < in-degree <= split (work order)
 };
 
 // Launch helpers implemented in level_kernels.cu / cta_kernel.cu.
@@ -164,14 +164,22 @@ struct CtaParams {
   const uint32_t* sources;
   uint32_t num_sources;
   uint32_t* dist;        // row s at dist + s * V (null when stats is set)
-  uint32_t* gqueue;      // per resident block: 2 * V u32
+  uint32_t* gqueue;      // per resident block: V u32
   uint32_t* work;        // source cursor (zeroed before launch)
   SourceStats* stats;    // non-null: per-source reductions instead of rows
+  uint32_t* gbits;       // global-bitmap mode: per resident block ceil(V/32) u32
 };
-// Max V for the shared-memory visited bitmap; grid/block for the CTA kernel.
+struct CtaShape {
+  int grid = 0;           // resident blocks
+  int block = 0;          // threads per block
+  size_t smem = 0;        // dynamic shared memory (the bitmap in shared mode)
+  bool global_bits = false;
+};
+// Max V for the shared-memory visited bitmap; launch shape of the CTA kernel
+// (global-bitmap mode above that V when allow_global).
 size_t cta_max_vertices(int device);
-bool cta_launch_shape(uint32_t V, int device, int* grid, int* block, size_t* smem);
-void launch_cta(const CtaParams& p, int grid, int block, size_t smem, cudaStream_t s);
+bool cta_launch_shape(uint32_t V, int device, bool allow_global, CtaShape* out);
+void launch_cta(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s);
 
 void launch_traversed_edges(uint32_t V, const uint32_t* off, const uint32_t* dist,
                             uint32_t num_sources, unsigned long long* out, cudaStream_t s);

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -39,7 +40,8 @@ struct Workspace;
 
 struct msbfs_graph {
   msbfs_engine* eng = nullptr;
-  uint64_t id = 0;
+  std::vector<msbfs_engine*> users;  // other engines of the device that may run on it
+  uint64_t id = 0;  // unique in the process: keys every engine's workspaces
   size_t V = 0, E = 0;
   bool sym = false;
   uint32_t max_deg = 0;
@@ -52,8 +54,7 @@ struct msbfs_graph {
   uint32_t n_heavy = 0;
   uint32_t n_hchunks = 0;
   HeavyChunk* hchunks = nullptr;
-  // Bottom-up work order: vertices with 0 < in-degree <= split, in-degree
-  // descending, ids ascending within a degree.
+  // Bottom-up work order: vertices with 0 < in-degree <= split, ascending ids.
   uint32_t n_order = 0;
   uint32_t* order = nullptr;
 };
@@ -124,8 +125,12 @@ struct msbfs_engine {
   uint32_t beta = 24;
   uint32_t seg = 64;
   uint32_t heavy = 32;
-  uint32_t split = 256;
+#ifndef MSBFS_SPLIT
+#define MSBFS_SPLIT 256
+#endif
+  uint32_t split = MSBFS_SPLIT;  // in-edge slice length of bottom-up steps
   uint32_t bits_div = 64;
+  uint32_t sm_share = 100;  // percent of the resident grid the persistent kernels use
   bool host_loop = false;
   bool zero_copy = true;  // MSBFS_ZERO_COPY=0 stages host output in HBM instead
   int profiling = 0;
@@ -134,7 +139,6 @@ struct msbfs_engine {
   size_t h_log_passes = 0;
   std::vector<cudaEvent_t> lvl_events;       // profiling level 2
   std::vector<std::vector<float>> pass_event_ms;
-  uint64_t next_graph_id = 1;
   std::map<std::tuple<uint64_t, uint32_t, uint32_t>, std::unique_ptr<Workspace>> ws;
   // call scratch
   uint32_t* d_sources = nullptr;
@@ -145,6 +149,8 @@ struct msbfs_engine {
   size_t d_reach_cap = 0;
   uint32_t* d_cta_queue = nullptr;
   size_t d_cta_queue_cap = 0;
+  uint32_t* d_cta_bits = nullptr;  // global-bitmap mode of the CTA path
+  size_t d_cta_bits_cap = 0;
   uint32_t* d_work = nullptr;
   unsigned long long* d_counter = nullptr;
   SourceStats* d_sstats = nullptr;  // per-source reductions of host-output calls
@@ -299,6 +305,9 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   w->mode = mode;
   if (!level_kernel_info(W, eng->num_sms, &w->k))
     return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "unsupported words per vertex");
+  // Work is claimed dynamically, so a smaller grid is only slower, never wrong.
+  w->k.level_grid = std::max(1, (int)((uint64_t)w->k.level_grid * eng->sm_share / 100));
+  w->k.mat_grid = std::max(1, (int)((uint64_t)w->k.mat_grid * eng->sm_share / 100));
   LevelParams& p = w->p;
   p.V = (uint32_t)g->V;
   p.W = W;
@@ -452,7 +461,8 @@ uint32_t choose_words(msbfs_engine* eng, size_t S) {
 int validate_call(msbfs_engine* eng, const msbfs_graph* g, const uint32_t* sources, size_t S) {
   if (!eng) return MSBFS_ERR_INVALID_ARGUMENT;
   if (!g) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "graph is null");
-  if (g->eng != eng) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "graph belongs to another engine");
+  if (g->eng != eng && std::find(g->users.begin(), g->users.end(), eng) == g->users.end())
+    return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "graph belongs to another engine");
   if (S == 0) return MSBFS_OK;
   if (!sources) return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "sources is null");
   char buf[160];
@@ -495,11 +505,10 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   const int m = resolve_method(g, method, S);
   uint32_t path = method_path(m);
   if (reach_dev && path == MSBFS_PATH_CTA) path = MSBFS_PATH_HYBRID;
-  int cta_grid = 0, cta_block = 0;
-  size_t cta_smem = 0;
-  if (path == MSBFS_PATH_CTA &&
-      !cta_launch_shape((uint32_t)g->V, eng->device, &cta_grid, &cta_block, &cta_smem))
+  CtaShape cta{};
+  if (path == MSBFS_PATH_CTA && !cta_launch_shape((uint32_t)g->V, eng->device, true, &cta))
     path = MSBFS_PATH_HYBRID;
+  const int cta_grid = std::max(1, (int)((uint64_t)cta.grid * eng->sm_share / 100));
   if (!g->sym && path != MSBFS_PATH_CTA && !g->coff)
     return set_err(eng, MSBFS_ERR_INVALID_GRAPH, "missing transpose");
 
@@ -514,8 +523,12 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   const size_t V = g->V;
 
   if (path == MSBFS_PATH_CTA) {
-    const size_t slabs = (size_t)cta_grid * 2 * V;
-    if ((rc = grow(eng, &eng->d_cta_queue, &eng->d_cta_queue_cap, slabs))) return rc;
+    const int blocks = std::min<int>(cta_grid, (int)S);
+    if ((rc = grow(eng, &eng->d_cta_queue, &eng->d_cta_queue_cap, (size_t)blocks * V)))
+      return rc;
+    if (cta.global_bits &&
+        (rc = grow(eng, &eng->d_cta_bits, &eng->d_cta_bits_cap, (size_t)blocks * ((V + 31) / 32))))
+      return rc;
     CK(cudaMemsetAsync(eng->d_work, 0, sizeof(uint32_t), eng->stream));
     CtaParams cp{};
     cp.V = (uint32_t)V;
@@ -527,7 +540,8 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     cp.gqueue = eng->d_cta_queue;
     cp.work = eng->d_work;
     cp.stats = stats_dev;
-    launch_cta(cp, std::min<int>(cta_grid, (int)S), cta_block, cta_smem, eng->stream);
+    cp.gbits = cta.global_bits ? eng->d_cta_bits : nullptr;
+    launch_cta(cp, cta, blocks, eng->stream);
     CK(cudaGetLastError());
     eng->last.passes = 1;
     eng->last_passes = 0;
@@ -678,7 +692,8 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
   if (!why.empty()) return set_err(eng, MSBFS_ERR_INVALID_GRAPH, why);
   auto g = std::make_unique<msbfs_graph>();
   g->eng = eng;
-  g->id = eng->next_graph_id++;
+  static std::atomic<uint64_t> next_graph_id{1};
+  g->id = next_graph_id++;
   g->V = V;
   g->E = E;
   g->max_deg = msbfs::max_degree(V, off);
@@ -718,25 +733,31 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
   if (!chunks.empty())
     CK(cudaMemcpy(g->hchunks, chunks.data(), chunks.size() * sizeof(HeavyChunk),
                   cudaMemcpyHostToDevice));
-  // Bottom-up work list: the vertices with 0 < in-degree <= split. Ascending
-  // ids by default (neighbouring vertices share cache lines of the visited and
-  // frontier rows); MSBFS_ORDER_BY_ID=0 sorts by in-degree, descending, which
-  // measured ~7% slower on R-MAT scale 22.
+  // Bottom-up work list: the vertices with 0 < in-degree <= split, ascending
+  // ids (neighbouring vertices share cache lines of the visited and frontier
+  // rows). MSBFS_ORDER_WINDOW > 1 sorts by in-degree, descending, within
+  // windows of that many entries, so the groups of a warp scan in-edge lists
+  // of similar length; on R-MAT scale 22, S=512 the lost locality outweighs
+  // the balance (window 256: +8%, window 1024: +10% bottom-up time), so the
+  // default keeps plain id order.
   {
-#ifndef MSBFS_ORDER_BY_ID
-#define MSBFS_ORDER_BY_ID 1
+#ifndef MSBFS_ORDER_WINDOW
+#define MSBFS_ORDER_WINDOW 0
 #endif
-    auto key = [&](uint32_t d) { return MSBFS_ORDER_BY_ID ? 0u : g->split - d; };
-    std::vector<uint32_t> start(g->split + 2, 0);
+    std::vector<uint32_t> order;
+    order.reserve(V);
     for (size_t v = 0; v < V; ++v) {
       const uint32_t d = t.off[v + 1] - t.off[v];
-      if (d > 0 && d <= g->split) start[key(d) + 1]++;
+      if (d > 0 && d <= g->split) order.push_back((uint32_t)v);
     }
-    for (uint32_t i = 1; i < start.size(); ++i) start[i] += start[i - 1];
-    std::vector<uint32_t> order(start.back());
-    for (size_t v = 0; v < V; ++v) {
-      const uint32_t d = t.off[v + 1] - t.off[v];
-      if (d > 0 && d <= g->split) order[start[key(d)]++] = (uint32_t)v;
+    const size_t win = MSBFS_ORDER_WINDOW;
+    if (win > 1) {
+      auto deg_desc = [&](uint32_t a, uint32_t b) {
+        return t.off[a + 1] - t.off[a] > t.off[b + 1] - t.off[b];
+      };
+      for (size_t i = 0; i < order.size(); i += win)
+        std::stable_sort(order.begin() + i, order.begin() + std::min(order.size(), i + win),
+                         deg_desc);
     }
     g->n_order = (uint32_t)order.size();
     CK(cudaMalloc((void**)&g->order, std::max<size_t>(order.size(), 1) * 4));
@@ -749,8 +770,10 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
 
 void free_graph(msbfs_graph* g) {
   if (!g) return;
-  msbfs_engine* eng = g->eng;
-  if (eng) {
+  std::vector<msbfs_engine*> engines = g->users;
+  engines.push_back(g->eng);
+  for (msbfs_engine* eng : engines) {
+    if (!eng) continue;
     std::lock_guard<std::mutex> lk(eng->mu);
     cudaSetDevice(eng->device);
     cudaStreamSynchronize(eng->stream);
@@ -785,8 +808,7 @@ int run_host(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t
   // segments, instead of being staged in HBM and copied afterwards. The
   // CTA-per-source path stores 4-byte distances as it discovers them, which
   // the host link serves ~9x slower than a staged copy, so it keeps staging.
-  const bool cta = method_path(resolve_method(g, method, S)) == MSBFS_PATH_CTA &&
-                   cta_max_vertices(eng->device) >= g->V;
+  const bool cta = method_path(resolve_method(g, method, S)) == MSBFS_PATH_CTA;
   if (eng->zero_copy && !cta) {
     cudaPointerAttributes attr{};
     if (cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
@@ -854,6 +876,7 @@ void msbfs_engine_destroy(msbfs_engine* e) {
   cudaFree(e->d_dist);
   cudaFree(e->d_reach);
   cudaFree(e->d_cta_queue);
+  cudaFree(e->d_cta_bits);
   cudaFree(e->d_work);
   cudaFree(e->d_counter);
   cudaFree(e->d_sstats);
@@ -898,6 +921,18 @@ int msbfs_engine_set_tuning(msbfs_engine* e, uint32_t max_words, uint32_t alpha,
   return MSBFS_OK;
 }
 
+int msbfs_engine_set_sm_share(msbfs_engine* e, uint32_t percent) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (percent < 1 || percent > 100)
+    return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "sm share must be 1..100 percent");
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->sm_share = percent;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->stream);
+  e->ws.clear();  // grid sizes are baked into the captured graphs
+  return MSBFS_OK;
+}
+
 int msbfs_engine_set_profiling(msbfs_engine* e, int level) {
   if (!e || level < 0 || level > 2) return MSBFS_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(e->mu);
@@ -930,6 +965,23 @@ int msbfs_graph_create(msbfs_engine* e, size_t V, size_t E, const uint32_t* off,
 }
 
 void msbfs_graph_destroy(msbfs_graph* g) { free_graph(g); }
+
+}  // extern "C"
+
+// Lets another engine of the same device run on `g` without a second upload
+// (the served form's slots share one resident graph). Not part of the C ABI:
+// destroying `g` drops the workspaces of every engine attached to it, so `g`
+// must be destroyed before any of them.
+int msbfs_graph_attach(msbfs_graph* g, msbfs_engine* e) {
+  if (!g || !e || !g->eng) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (e->device != g->eng->device)
+    return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "graph lives on another device");
+  if (e != g->eng && std::find(g->users.begin(), g->users.end(), e) == g->users.end())
+    g->users.push_back(e);
+  return MSBFS_OK;
+}
+
+extern "C" {
 
 int msbfs_graph_info(const msbfs_graph* g, size_t* V, size_t* E, uint32_t* max_deg, int* sym) {
   if (!g) return MSBFS_ERR_INVALID_ARGUMENT;

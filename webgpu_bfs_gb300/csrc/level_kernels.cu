@@ -374,19 +374,39 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     if (!__any_sync(FULL, any_bits<VEC>(needed))) continue;
     if (hk.j == 0 && lane == 0) cnt.active += 1;
     if (!__all_sync(FULL, sat)) {
+      // Each round the warp gathers GPW*CH in-neighbours; the ids of the next
+      // round are fetched while this round's frontier rows are in flight, so
+      // a round costs one memory latency, not two.
+      constexpr int NI = LPV >= CH ? 1 : CH;  // ids held per lane
+      uint32_t ids[NI];
+#pragma unroll
+      for (int j = 0; j < NI; ++j) {
+        const uint32_t e = beg + gid * CH + (LPV >= CH ? lig : j);
+        ids[j] = ((LPV < CH || lig < CH) && e < end) ? __ldg(in_idx + e) : FULL;
+      }
       for (uint32_t base = beg; base < end; base += GPW * CH) {
         const uint32_t e0 = base + gid * CH;
         if (lig == 0 && e0 < end) cnt.edges += min((uint32_t)CH, end - e0);
+        uint32_t u[CH];
+        if constexpr (LPV >= CH) {
+#pragma unroll
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, ids[0], gbase + j);
+        } else {
+#pragma unroll
+          for (int j = 0; j < CH; ++j) u[j] = ids[j];
+        }
+#pragma unroll
+        for (int j = 0; j < NI; ++j) {
+          const uint32_t e = e0 + GPW * CH + (LPV >= CH ? lig : j);
+          ids[j] = ((LPV < CH || lig < CH) && e < end) ? __ldg(in_idx + e) : FULL;
+        }
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (e0 + j < end) {
-            const uint32_t u = __ldg(in_idx + e0 + j);
-            if (in_frontier(fb, u)) {
-              cnt.rows += 1;
-              Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
+          if (u[j] != FULL && in_frontier(fb, u[j])) {
+            cnt.rows += 1;
+            Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
 #pragma unroll
-              for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
-            }
+            for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
           }
         }
         bool s2 = true;
@@ -429,10 +449,10 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
   }
 
   // ---- (2) all other vertices with in-edges, in the graph's work order
-  // (in-degree descending, ids ascending within a degree), so the groups of a
-  // warp walk in-edge lists of equal length and vertices without in-edges
-  // cost nothing. Tiles are claimed dynamically: the expensive vertices come
-  // first and a static split would leave most warps idle behind a few.
+  // (ascending ids: neighbouring vertices share cache lines of the visited
+  // and frontier rows), so vertices without in-edges cost nothing. Tiles are
+  // claimed dynamically: work concentrates at some ids (R-MAT puts its hubs
+  // first) and a static split would leave most warps idle behind a few.
   const uint32_t ntiles = (p.n_order + GPW - 1) / GPW;
   uint32_t tile = 0, tile_end = 0;
   for (;;) {
@@ -527,19 +547,36 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         hneed.w[q] = __shfl_sync(FULL, needed.w[q], hl + lig);
         hc.w[q] = 0;
       }
+      constexpr int NI = LPV >= CH ? 1 : CH;  // ids held per lane (next round)
+      uint32_t ids[NI];
+#pragma unroll
+      for (int j = 0; j < NI; ++j) {
+        const uint32_t e = hbeg + gid * CH + (LPV >= CH ? lig : j);
+        ids[j] = ((LPV < CH || lig < CH) && e < hend) ? __ldg(in_idx + e) : FULL;
+      }
       for (uint32_t base = hbeg; base < hend; base += GPW * CH) {
         const uint32_t e0 = base + gid * CH;
         if (lig == 0 && e0 < hend) cnt.edges += min((uint32_t)CH, hend - e0);
+        uint32_t u[CH];
+        if constexpr (LPV >= CH) {
+#pragma unroll
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, ids[0], gbase + j);
+        } else {
+#pragma unroll
+          for (int j = 0; j < CH; ++j) u[j] = ids[j];
+        }
+#pragma unroll
+        for (int j = 0; j < NI; ++j) {
+          const uint32_t e = e0 + GPW * CH + (LPV >= CH ? lig : j);
+          ids[j] = ((LPV < CH || lig < CH) && e < hend) ? __ldg(in_idx + e) : FULL;
+        }
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (e0 + j < hend) {
-            const uint32_t u = __ldg(in_idx + e0 + j);
-            if (in_frontier(fb, u)) {
-              cnt.rows += 1;
-              Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
+          if (u[j] != FULL && in_frontier(fb, u[j])) {
+            cnt.rows += 1;
+            Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
 #pragma unroll
-              for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
-            }
+            for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
           }
         }
         bool sat = true;
@@ -817,14 +854,10 @@ __global__ void init_kernel(LevelParams p) {
 
 __device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __clz(x) : 0; }
 
-// Turns visited words + level planes into the source-major u32 distance rows
-// (or copies the visited words out as a reachability bitmask), and zeroes the
-// words it read so the next pass starts from clean buffers. A block stages a
-// tile of MAT_TV consecutive vertices x KC words in shared memory (word-major,
-// so a lane reads its 4 vertices with one 16-byte load); warp c then owns word
-// c: it keeps the tile's visited/plane words of its 4 vertices in registers
-// and writes the 32 rows s = 32*(kb+c) + j as 512-byte contiguous segments
-// (one 16-byte store per lane per row).
+// Materialisation: a work item is word c (sources 32c .. 32c+31 of the
+// pass) of MAT_TV consecutive vertices, 4 per lane, so each distance row is
+// written with 16-byte stores (one vertex per lane with 4-byte stores
+// measured 1.6x slower on R-MAT scale 22, S=512, despite more resident warps).
 constexpr int MAT_TV = 128;  // vertices per work item (4 per lane)
 constexpr int MAT_NPMAX = 8;
 

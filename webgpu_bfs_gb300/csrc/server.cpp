@@ -18,6 +18,9 @@
 
 #include "../../include/msbfs.h"
 
+// engine.cu: lets a second engine of the device run on a resident graph.
+int msbfs_graph_attach(msbfs_graph* g, msbfs_engine* e);
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -56,6 +59,7 @@ struct Slot {
   size_t h_stage_bytes = 0;
   std::vector<Part> parts;
   int mode = MSBFS_SERVE_STATS;
+  bool express = false;  // takes small requests only, narrow launches
   bool busy = false;
   int launch_rc = MSBFS_OK;
 };
@@ -70,6 +74,7 @@ struct msbfs_server {
   int device = 0;
   size_t V = 0;
   msbfs_server_config cfg{};
+  msbfs_graph* graph = nullptr;  // resident once, owned by slot 0's engine
   std::vector<Slot> slots;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -77,6 +82,7 @@ struct msbfs_server {
   std::map<uint64_t, std::unique_ptr<Request>> reqs;
   uint64_t next_id = 1;
   bool stop = false;
+  uint64_t traversals = 0, kernel_launches = 0;
   std::thread sched;
 };
 
@@ -154,6 +160,14 @@ void scheduler(msbfs_server* s) {
           rc = MSBFS_ERR_CUDA;
         }
       }
+      if (!rc) {
+        // Already complete: collects the traversal's status and level count.
+        msbfs_stats st{};
+        rc = msbfs_engine_synchronize(sl.eng, &st);
+        s->traversals++;
+        s->kernel_launches +=
+            st.path == MSBFS_PATH_CTA ? 1 : (uint64_t)(st.levels + 3) * st.passes;
+      }
       const size_t eb = elem_bytes(sl.mode, s->V);
       for (const Part& p : sl.parts) {
         if (!rc && !p.r->out_pinned)
@@ -165,23 +179,52 @@ void scheduler(msbfs_server* s) {
       sl.busy = false;
       progress = true;
     }
-    // Admissions: the next free slot takes queued requests of the head's
-    // output mode, in arrival order, until its lanes (and, for rows, its
-    // staging bytes) are used up; larger requests continue in later launches.
+    // Admissions: the next free slot takes queued requests of one output
+    // mode, in arrival order, until its lanes (and, for rows, its staging
+    // bytes) are used up; larger requests continue in later launches. An
+    // express slot takes small requests only; a general slot takes large
+    // requests first when express slots exist, small ones only when no large
+    // request waits.
+    const size_t small = s->cfg.small_sources;
     for (Slot& sl : s->slots) {
       if (sl.busy || s->queue.empty()) continue;
-      sl.mode = s->queue.front()->mode;
+      const bool have_express = s->cfg.express_slots > 0;
+      bool want_small = sl.express;
+      const Request* head = nullptr;
+      for (const Request* r : s->queue) {
+        const bool is_small = r->src.size() <= small;
+        if (sl.express ? is_small : (!have_express || !is_small)) {
+          head = r;
+          break;
+        }
+      }
+      if (!head && !sl.express) {  // no large request waits: take small ones
+        head = s->queue.front();
+        want_small = true;
+      }
+      if (!head) continue;
+      sl.mode = head->mode;
       size_t cap = s->cfg.max_sources_per_launch;
+      if (sl.express) cap = std::min(cap, 2 * small);
       if (sl.mode == MSBFS_SERVE_ROWS) cap = std::min(cap, sl.rows_cap);
       std::vector<uint32_t> lanes;
       const auto now = Clock::now();
       for (size_t i = 0; i < s->queue.size() && lanes.size() < cap;) {
         Request* r = s->queue[i];
-        if (r->mode != sl.mode) {
+        const bool is_small = r->src.size() <= small;
+        const bool eligible = sl.express ? is_small
+                              : (!have_express || want_small) ? true
+                                                              : !is_small;
+        if (r->mode != sl.mode || !eligible) {
           ++i;
           continue;
         }
-        const size_t take = std::min(r->src.size() - r->next, cap - lanes.size());
+        const size_t left = r->src.size() - r->next;
+        if (sl.express && !lanes.empty() && left > cap - lanes.size()) {
+          ++i;  // a small request is not split while a later launch can hold it whole
+          continue;
+        }
+        const size_t take = std::min(left, cap - lanes.size());
         sl.parts.push_back(Part{r, r->next, take, lanes.size()});
         lanes.insert(lanes.end(), r->src.begin() + r->next, r->src.begin() + r->next + take);
         r->next += take;
@@ -211,9 +254,12 @@ void scheduler(msbfs_server* s) {
 }
 
 void destroy_slots(msbfs_server* s) {
-  for (Slot& sl : s->slots) {
+  for (Slot& sl : s->slots)
     if (sl.stream) cudaStreamSynchronize(sl.stream);
-    if (sl.g) msbfs_graph_destroy(sl.g);
+  // The shared graph goes first: it drops every attached engine's workspaces.
+  if (s->graph) msbfs_graph_destroy(s->graph);
+  s->graph = nullptr;
+  for (Slot& sl : s->slots) {
     if (sl.eng) msbfs_engine_destroy(sl.eng);
     if (sl.d_rows) cudaFree(sl.d_rows);
     if (sl.d_stats) cudaFree(sl.d_stats);
@@ -241,25 +287,41 @@ int msbfs_server_create(int device, size_t V, size_t E, const uint32_t* ro, cons
   if (s->cfg.slots == 0) s->cfg.slots = 2;
   if (s->cfg.max_sources_per_launch == 0) s->cfg.max_sources_per_launch = 512;
   if (s->cfg.hbm_budget_bytes == 0) s->cfg.hbm_budget_bytes = 8ull << 30;
-  if (s->cfg.method < 0 || s->cfg.method > MSBFS_METHOD_AUTO) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (s->cfg.small_sources == 0) s->cfg.small_sources = 64;
+  if (s->cfg.general_sm_percent == 0) s->cfg.general_sm_percent = 100;
+  if (s->cfg.method < 0 || s->cfg.method > MSBFS_METHOD_AUTO ||
+      s->cfg.express_slots >= s->cfg.slots || s->cfg.general_sm_percent > 100 ||
+      s->cfg.reserved != 0)
+    return MSBFS_ERR_INVALID_ARGUMENT;
   if (cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
     return MSBFS_ERR_NO_DEVICE;
   }
+  int prio_low = 0, prio_high = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
   const size_t per_slot = s->cfg.hbm_budget_bytes / s->cfg.slots;
   const size_t rows_cap =
       std::max<size_t>(1, std::min<size_t>(s->cfg.max_sources_per_launch, per_slot / (V * 4)));
   s->slots.resize(s->cfg.slots);
   int rc = MSBFS_OK;
-  for (Slot& sl : s->slots) {
+  for (size_t k = 0; k < s->slots.size(); ++k) {
+    Slot& sl = s->slots[k];
+    sl.express = k < s->cfg.express_slots;
     if ((rc = msbfs_engine_create(device, s->cfg.method, &sl.eng))) break;
-    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking,
+                                     sl.express ? prio_high : prio_low) != cudaSuccess ||
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
       rc = MSBFS_ERR_CUDA;
       break;
     }
     if ((rc = msbfs_engine_set_stream(sl.eng, sl.stream))) break;
-    if ((rc = msbfs_graph_create(sl.eng, V, E, ro, ci, &sl.g))) break;
+    if (!sl.express && s->cfg.general_sm_percent < 100 &&
+        (rc = msbfs_engine_set_sm_share(sl.eng, s->cfg.general_sm_percent)))
+      break;
+    // One resident copy of the graph, shared by every slot's engine.
+    if (k == 0 && (rc = msbfs_graph_create(sl.eng, V, E, ro, ci, &s->graph))) break;
+    if ((rc = msbfs_graph_attach(s->graph, sl.eng))) break;
+    sl.g = s->graph;
     sl.rows_cap = rows_cap;
     if (cudaMalloc((void**)&sl.d_rows, rows_cap * V * 4) != cudaSuccess ||
         cudaMalloc((void**)&sl.d_stats,
@@ -333,6 +395,14 @@ int msbfs_server_wait(msbfs_server* s, uint64_t ticket, double timeout_ms,
   }
   s->reqs.erase(it);
   return st;
+}
+
+int msbfs_server_counters(msbfs_server* s, uint64_t* traversals, uint64_t* kernel_launches) {
+  if (!s) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (traversals) *traversals = s->traversals;
+  if (kernel_launches) *kernel_launches = s->kernel_launches;
+  return MSBFS_OK;
 }
 
 void msbfs_server_destroy(msbfs_server* s) {
