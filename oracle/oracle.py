@@ -146,3 +146,124 @@ def is_symmetric(V: int, row_offsets, col_indices) -> bool:
     ro, ci = _u32(row_offsets), _u32(col_indices)
     E = ci.size
     return bool(lib().oracle_is_symmetric(V, E, _p(ro), _p(ci if E else np.zeros(1, np.uint32))))
+
+
+class MtxOracleError(ValueError):
+    """A rejected Matrix Market text: ``kind`` names the MtxError variant
+    (crates/core/src/error.rs:43-81), ``line`` its line number (0: none)."""
+
+    def __init__(self, kind: str, line: int, message: str):
+        super().__init__(message)
+        self.kind, self.line = kind, line
+
+
+def _rust_usize(tok: str):
+    """usize::from_str: optional '+', ASCII digits, 64-bit range."""
+    body = tok[1:] if tok.startswith("+") else tok
+    if tok == "":
+        return None, "cannot parse integer from empty string"
+    if body == "" or not all("0" <= ch <= "9" for ch in body):
+        return None, "invalid digit found in string"
+    v = int(body)
+    if v >= 1 << 64:
+        return None, "number too large to fit in target type"
+    return v, None
+
+
+def mtx_parse(text: str):
+    """MtxReader::parse (crates/core/src/mtx.rs:124-275), line by line like the
+    reference -> (V, row_offsets, col_indices); raises MtxOracleError."""
+    lines = text.split("\n")
+    if lines and lines[-1] == "":
+        lines.pop()  # BufRead::lines yields no empty line after the last newline
+    i = 0
+
+    def nxt():
+        nonlocal i
+        if i >= len(lines):
+            i += 1
+            return None
+        s = lines[i].strip(" \t\r\n\v\f")
+        i += 1
+        return s
+
+    while True:
+        s = nxt()
+        if s is None:
+            raise MtxOracleError("InvalidHeader", i, f"Invalid Matrix Market header at line {i}: "
+                                 "Empty input: no MatrixMarket header found")
+        if s:
+            break
+    t = s.split()
+    hdr = f"Invalid Matrix Market header at line {i}: "
+    if len(t) != 5:
+        raise MtxOracleError("InvalidHeader", i, hdr + f"Expected 5 tokens in header line, "
+                             f"found {len(t)}: '{s}'")
+    if t[0].lower() != "%%matrixmarket":
+        raise MtxOracleError("InvalidHeader", i, hdr + f"Missing '%%MatrixMarket' banner: "
+                             f"'{t[0]}'")
+    if t[1].lower() != "matrix":
+        raise MtxOracleError("InvalidHeader", i, hdr + f"Unsupported object '{t[1]}', only "
+                             "'matrix' is supported")
+    fmt, field, sym = t[2].lower(), t[3].lower(), t[4].lower()
+    if fmt == "array":
+        raise MtxOracleError("UnsupportedFormat", 0, "Unsupported Matrix Market format "
+                             "'array': only sparse 'coordinate' format is supported")
+    if fmt != "coordinate":
+        raise MtxOracleError("InvalidHeader", i, hdr + f"Unknown format '{fmt}'")
+    if field not in ("pattern", "real", "integer", "complex"):
+        raise MtxOracleError("InvalidHeader", i, hdr + f"Unknown field '{field}'")
+    if sym not in ("general", "symmetric", "skew-symmetric", "hermitian"):
+        raise MtxOracleError("InvalidHeader", i, hdr + f"Unknown symmetry '{sym}'")
+    symmetric = sym != "general"
+    while True:
+        s = nxt()
+        if s is None:
+            raise MtxOracleError("InvalidDimensions", i, f"Invalid dimensions at line {i}: "
+                                 "Unexpected end of file while searching for dimension line")
+        if s and not s.startswith("%"):
+            break
+    t = s.split()
+    dim = f"Invalid dimensions at line {i}: "
+    if len(t) != 3:
+        raise MtxOracleError("InvalidDimensions", i, dim + "Expected 3 integer tokens (rows "
+                             f"cols nnz), got {len(t)}: '{s}'")
+    vals = []
+    for name, tok in zip(("rows", "cols", "nnz"), t):
+        v, why = _rust_usize(tok)
+        if why:
+            raise MtxOracleError("InvalidDimensions", i, dim + f"Failed to parse {name} count "
+                                 f"'{tok}': {why}")
+        vals.append(v)
+    rows, cols, _ = vals
+    if symmetric and rows != cols:
+        raise MtxOracleError("InvalidDimensions", i, dim + "Symmetric matrix must be square, "
+                             f"but got {rows} rows and {cols} cols")
+    edges = []
+    while i < len(lines):
+        s = nxt()
+        if not s or s.startswith("%"):
+            continue
+        t = s.split()
+        if len(t) < 2:
+            raise MtxOracleError("InvalidCoordinateLine", i,
+                                 f"Invalid coordinate entry at line {i}: '{s}'")
+        r, e1 = _rust_usize(t[0])
+        c, e2 = _rust_usize(t[1])
+        if e1 or e2:
+            raise MtxOracleError("InvalidCoordinateLine", i,
+                                 f"Invalid coordinate entry at line {i}: '{s}'")
+        if r == 0 or c == 0:
+            raise MtxOracleError("ZeroIndex", i, "Matrix Market coordinates are 1-based, but "
+                                 f"found 0 at line {i}: row={r}, col={c}")
+        if r > rows or c > cols:
+            raise MtxOracleError("IndexOutOfBounds", i, f"Coordinate out of bounds at line {i}: "
+                                 f"entry ({r}, {c}) exceeds matrix dimensions ({rows}, {cols})")
+        if r == c:
+            continue
+        edges.append((r - 1, c - 1))
+        if symmetric:
+            edges.append((c - 1, r - 1))
+    V = max(rows, cols)
+    ro, ci = csr_from_edge_list(V, edges if edges else np.zeros((0, 2), np.uint32))
+    return V, ro, ci
