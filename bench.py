@@ -438,6 +438,11 @@ def run_ours(args, spec):
             "materialize": mat,
             "cpu_baseline": cpu,
         }
+        if world == 1 and args.workload == "rmat22_s512" and not args.no_forms:
+            del out  # the forms allocate their own device buffers
+            torch.cuda.empty_cache()
+            eng.close()
+            res["forms"] = forms_summary()
         print(json.dumps(res), flush=True)
     eng.close()
     if world > 1:
@@ -468,50 +473,96 @@ def make_batch(m, spec):
     return items
 
 
-def run_batched(args, spec):
-    """Batched form vs the plain per-graph launch loop, both device-timed."""
-    import torch
-    import __graft_entry__
-    __graft_entry__.build()
-    import webgpu_bfs_gb300 as m
+def batched_experiment(m, spec, steps, warmup):
+    """Batched form (one persistent launch over every graph) vs the plain
+    per-graph launch loop, both device-timed."""
     t0 = time.perf_counter()
     items = make_batch(m, spec)
     gen_s = time.perf_counter() - t0
-    total_src = sum(int(s.size) for _, s in items)
-    total_v = sum(g.num_vertices for g, _ in items)
     b = m.BatchedBfs(items)
-    t0 = time.perf_counter()
-    b.autotune(samples_per_class=3)
-    tune_s = time.perf_counter() - t0
-    for _ in range(max(1, args.warmup)):
-        b.run()
-        b.run_per_graph()
+    try:
+        t0 = time.perf_counter()
+        b.autotune(samples_per_class=3)
+        tune_s = time.perf_counter() - t0
+        for _ in range(max(1, warmup)):
+            b.run()
+            b.run_per_graph()
+        with ClockSampler(0) as clk:
+            batched = [b.run() for _ in range(steps)]
+        plain = [b.run_per_graph() for _ in range(steps)]
+        classes = {}
+        for i in range(len(items)):
+            c = b.config(i)
+            classes[c["class"]] = {k: c[k] for k in ("alg", "words", "param")}
+    finally:
+        b.close()
+    return {"items": items, "batched_ms": batched, "plain_ms": plain, "gen_s": gen_s,
+            "tune_s": tune_s, "classes": classes, "clocks": clk.summary(),
+            "sources": sum(int(s.size) for _, s in items),
+            "vertices": sum(g.num_vertices for g, _ in items)}
+
+
+def run_batched(args, spec):
+    import __graft_entry__
+    __graft_entry__.build()
+    import webgpu_bfs_gb300 as m
     steps = max(1, min(args.steps, 10))
-    with ClockSampler(0) as clk:
-        batched = [b.run() for _ in range(steps)]
-    plain = [b.run_per_graph() for _ in range(steps)]
-    ms_b, ms_p = statistics.median(batched), statistics.median(plain)
-    classes = {}
-    for i in range(len(items)):
-        c = b.config(i)
-        classes[c["class"]] = {k: c[k] for k in ("alg", "words", "param")}
+    r = batched_experiment(m, spec, steps, args.warmup)
+    ms_b, ms_p = statistics.median(r["batched_ms"]), statistics.median(r["plain_ms"])
+    total_src = r["sources"]
     res = {
         "metric": "batched MS-BFS sources/sec (1,000 graphs, one launch)",
         "value": total_src / (ms_b / 1000.0), "unit": "sources/s", "n_gpus": 1,
         "steps": steps, "warmup": args.warmup, "ms_per_step": ms_b,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
-        "config": {"workload": args.workload, "graphs": len(items), "sources": total_src,
-                   "vertices": total_v, "generation_s": round(gen_s, 1),
-                   "autotune_s": round(tune_s, 2), "classes": classes},
+        "config": {"workload": args.workload, "graphs": len(r["items"]), "sources": total_src,
+                   "vertices": r["vertices"], "generation_s": round(r["gen_s"], 1),
+                   "autotune_s": round(r["tune_s"], 2), "classes": r["classes"]},
         "plain_per_graph": {"value": total_src / (ms_p / 1000.0), "ms_per_step": ms_p},
         "speedup_vs_plain": ms_p / ms_b,
-        "p50_ms": ms_b, "p99_ms": float(np.percentile(batched, 99)),
-        "clocks": clk.summary(),
+        "p50_ms": ms_b, "p99_ms": float(np.percentile(r["batched_ms"], 99)),
+        "clocks": r["clocks"],
         "gpu_launches": 1,
     }
     print(json.dumps(res), flush=True)
-    b.close()
+
+
+def forms_summary():
+    """Served and batched forms against the plain one-request-per-launch path,
+    in bounded time, for the default bench line: the batched configuration
+    (1,000 graphs, 5 timed launches of each kind) and the served form on the
+    resident 1448 x 1448 road graph (120 requests: capacity of both paths and
+    one Poisson stream offered at half the served capacity)."""
+    import webgpu_bfs_gb300 as m
+    out = {}
+    try:
+        r = batched_experiment(m, WORKLOADS["batched1000"], 5, 2)
+        mb, mp = statistics.median(r["batched_ms"]), statistics.median(r["plain_ms"])
+        out["batched"] = {"workload": "batched1000", "sources_per_s": r["sources"] / mb * 1e3,
+                          "plain_sources_per_s": r["sources"] / mp * 1e3,
+                          "speedup_vs_plain": mp / mb, "ms": mb, "plain_ms": mp}
+    except Exception as ex:  # reported, not hidden
+        out["batched"] = {"error": repr(ex)[:300]}
+    try:
+        spec = WORKLOADS["served_road1448"]
+        g = make_graph(m, spec["graph"])
+        reqs = make_requests(g, 120, spec["seed"])
+        r = served_experiment(m, g, reqs, SERVED_CONFIG, fractions=(0.5,), seed=spec["seed"],
+                              warm=20)
+        pt = r["sweep"][0]
+        out["served"] = {
+            "workload": "served_road1448 (120 requests)",
+            "sources_per_s": r["served_capacity"],
+            "plain_sources_per_s": r["plain_capacity"],
+            "speedup_vs_plain": r["served_capacity"] / r["plain_capacity"],
+            "at_half_load": {"served": pt["served"], "plain": pt["plain"]},
+            "latency_alone_ms": r["latency_alone_ms"],
+            "identical_results": f"{r['identical_results']}/{r['compared_results']}",
+            "kernel_launches": r["kernel_launches"]}
+    except Exception as ex:  # reported, not hidden
+        out["served"] = {"error": repr(ex)[:300]}
+    return out
 
 
 def make_requests(g, n, seed):
@@ -609,6 +660,19 @@ def served_experiment(m, g, reqs, cfg, fractions=(0.3, 0.6, 0.9), seed=0, warm=4
         for r in reqs[:warm]:  # first use of each lane width builds its workspace
             eng.run_ms_bfs_stats(g, r)
         serve_stream(srv, reqs[:warm], np.zeros(min(warm, len(reqs))))
+        # latency floor: requests of each size alone on an idle GPU
+        alone = {}
+        for S in SERVED_SIZES:
+            rs = [r for r in reqs if r.size == S][:5]
+            if not rs:
+                continue
+            s_ms = [srv.wait(srv.submit(r, srv.STATS))[1]["latency_ms"] for r in rs]
+            p_ms = []
+            for r in rs:
+                t0 = time.perf_counter()
+                eng.run_ms_bfs_stats(g, r)
+                p_ms.append(1000.0 * (time.perf_counter() - t0))
+            alone[S] = {"served_ms": statistics.median(s_ms), "plain_ms": statistics.median(p_ms)}
         c0 = srv.counters()
         with ClockSampler(0) as clk:
             s_out, s_lat, s_span = serve_stream(srv, reqs, np.zeros(len(reqs)))
@@ -631,7 +695,7 @@ def served_experiment(m, g, reqs, cfg, fractions=(0.3, 0.6, 0.9), seed=0, warm=4
             "served_capacity": cap_s, "plain_capacity": cap_p,
             "served_saturated": dict(_latency_summary(s_lat, sizes), makespan_s=s_span),
             "plain_saturated": dict(_latency_summary(p_lat, sizes), makespan_s=p_span),
-            "sweep": sweep, "identical_results": same,
+            "sweep": sweep, "latency_alone_ms": alone, "identical_results": same,
             "compared_results": len(reqs) * (1 + len(fractions)),
             "traversals": c1["traversals"] - c0["traversals"],
             "kernel_launches": c1["kernel_launches"] - c0["kernel_launches"],
@@ -676,6 +740,7 @@ def run_served(args, spec):
         "speedup_vs_plain": r["served_capacity"] / r["plain_capacity"],
         "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"],
         "sweep": r["sweep"],
+        "latency_alone_ms": r["latency_alone_ms"],
         "best_sources_per_s_with_small_p99_le_20ms":
             max((p["served"]["sources_per_s"] for p in ok), default=None),
         "parity": f"{r['identical_results']}/{r['compared_results']} served results "
@@ -722,6 +787,8 @@ def main():
     ap.add_argument("--workload", default="rmat22_s512", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the served/batched summary of the default workload's line")
     ap.add_argument("--ncu-case", choices=["level", "materialize"],
                     help="one untimed run sized for an ncu capture: 'level' = the "
                          "workload in reachability mode (no S*V matrix) with the level "

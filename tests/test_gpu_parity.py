@@ -235,3 +235,30 @@ def test_cta_global_bitmap_beyond_shared_memory(native, oracle):
         assert np.array_equal(st["distance_sum"], np.where(fin, d, 0).sum(1))
     finally:
         eng.close()
+
+
+def test_cta_frontier_beyond_shared_queue(native, oracle):
+    """Frontiers larger than the shared-memory queue halves (4,096 entries)
+    continue in the global slab: a star (level-1 frontier of 29,999), wide
+    random trees and an Erdos-Renyi graph; the 2,000,000-vertex tree runs in
+    global-bitmap mode."""
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.WorkgroupPersistentBfs)
+    try:
+        cases = [(native.star_graph(30000), [0, 1, 29999]),
+                 (native.generate_random_tree(300000, 9), None),
+                 (native.generate_erdos_renyi_np(60000, 8.0 / 59999, 4), None),
+                 (native.generate_random_tree(2000000, 10), None),  # global bitmap
+                 # road-like grids (edge-record queue entries), sources at the
+                 # centre so the diamond-shaped frontiers outgrow the queue
+                 # halves: shared bitmap (1,690,000 vertices) and global bitmap
+                 (native.generate_grid2d(1300, 1300), [650 * 1300 + 650, 0]),
+                 (native.generate_grid2d(3000, 3000), [1500 * 3000 + 1500, 7])]
+        for g, src in cases:
+            if src is None:
+                src = native.sample_sources(g, 9, 2)
+            src = np.asarray(src, np.uint32)
+            got = eng.run_ms_bfs(g, src)
+            assert eng.last_stats["path"] == 4
+            assert_same(got, _oracle(oracle, g, src), g, src, f"CTA V={g.num_vertices}")
+    finally:
+        eng.close()

@@ -23,30 +23,74 @@ namespace msbfs {
 
 constexpr uint32_t CTA_DIST_MAX = 0xffffffffu;
 constexpr int CTA_THREADS = 512;
+constexpr int CTA_BLOCKS_PER_SM = 4;  // 2,048 threads: every thread slot of an SM
 // Global-bitmap mode keeps its per-block scratch (queue slab + bitmap) within
 // this many bytes by shrinking the grid.
 constexpr size_t CTA_GLOBAL_SCRATCH_BYTES = 4ull << 30;
+// Frontier entries per shared-memory queue half (16 KB of vertex ids, 32 KB
+// of edge ranges).
+constexpr uint32_t CTA_SMEM_QUEUE = 4096;
 
 // GB: the visited bitmap lives in an L2-resident global slab per block (for
 // graphs whose bitmap does not fit shared memory) instead of shared memory.
 //
-// Queue: one slab of V words per block. The frontiers of consecutive levels
-// are disjoint vertex sets, so |F_L| + |F_L+1| <= V: even levels read from
-// the front of the slab and append at the back, odd levels the reverse.
+// ER: the graph carries edge records {target, target's first edge, target's
+// end edge} (built once per road-like graph), and a queue entry holds the
+// edge range of a frontier vertex instead of its id. Expanding a vertex then
+// costs one dependent L2 round trip per level (its edge records) instead of
+// three (queue entry, offsets, adjacency): on a ~4,000-level road graph the
+// per-level latency chain is what a traversal's time is made of.
+//
+// Queue: the first p.qh entries of a level's frontier sit in shared memory
+// (two halves, by level parity), the rest in one global slab of V words per
+// block (vertex ids: an ER reader looks their offsets up). The frontiers of
+// consecutive levels are disjoint vertex sets, so |F_L| + |F_L+1| <= V: in
+// the slab even levels sit at the front and odd levels at the back.
 // Counters: level L appends through s_cnt[L % 3]; thread 0 clears
 // s_cnt[(L+1) % 3] during level L (last read right after the barrier of
 // level L-2), so a level needs one block barrier.
-template <bool GB>
-__global__ void __launch_bounds__(CTA_THREADS) cta_bfs_kernel(CtaParams p) {
-  extern __shared__ uint32_t smem_bits[];
+template <bool GB, bool ER>
+__global__ void __launch_bounds__(CTA_THREADS, CTA_BLOCKS_PER_SM) cta_bfs_kernel(CtaParams p) {
+  extern __shared__ __align__(16) uint32_t smem_dyn[];
   __shared__ uint32_t s_src_idx;
   __shared__ uint32_t s_cnt[3];
   __shared__ unsigned long long s_sum;
   __shared__ uint32_t s_reached;
   const uint32_t V = p.V;
   const uint32_t words = (V + 31) / 32;
-  uint32_t* bits = GB ? p.gbits + (size_t)blockIdx.x * words : smem_bits;
+  const uint32_t QH = p.qh;
+  uint32_t* bits = GB ? p.gbits + (size_t)blockIdx.x * words : smem_dyn;
+  // queue halves after the bitmap, 8-byte aligned: ER entries are (eb, ee)
+  uint32_t* sq = smem_dyn + (GB ? 0 : (words + 1) / 2 * 2);
+  uint2* sq2 = reinterpret_cast<uint2*>(sq);
   uint32_t* slab = p.gqueue + (size_t)blockIdx.x * V;
+  auto slab_at = [&](uint32_t lv, uint32_t i) -> uint32_t* {
+    return (lv & 1) ? slab + (V - 1 - i) : slab + i;
+  };
+  // Edge range [*eb, *ee) of entry i of the frontier of level `lv`.
+  auto q_get = [&](uint32_t lv, uint32_t i, uint32_t* eb, uint32_t* ee) {
+    if constexpr (ER) {
+      if (i < QH) {
+        const uint2 r = sq2[(lv & 1) * QH + i];
+        *eb = r.x;
+        *ee = r.y;
+        return;
+      }
+    }
+    const uint32_t u = i < QH ? sq[(lv & 1) * QH + i] : *slab_at(lv, i);
+    *eb = __ldg(p.off + u);
+    *ee = __ldg(p.off + u + 1);
+  };
+  auto q_put = [&](uint32_t lv, uint32_t i, uint32_t v, uint32_t eb, uint32_t ee) {
+    if (i < QH) {
+      if constexpr (ER)
+        sq2[(lv & 1) * QH + i] = make_uint2(eb, ee);
+      else
+        sq[(lv & 1) * QH + i] = v;
+    } else {
+      *slab_at(lv, i) = v;
+    }
+  };
 
   for (;;) {
     if (threadIdx.x == 0) {
@@ -64,7 +108,7 @@ __global__ void __launch_bounds__(CTA_THREADS) cta_bfs_kernel(CtaParams p) {
     if (threadIdx.x == 0) {
       bits[src >> 5] = 1u << (src & 31);
       if (row) row[src] = 0;
-      slab[0] = src;
+      q_put(0, 0, src, __ldg(p.off + src), __ldg(p.off + src + 1));
     }
     uint32_t n_in = 1;
     uint32_t level = 0, ecc = 0;
@@ -74,29 +118,49 @@ __global__ void __launch_bounds__(CTA_THREADS) cta_bfs_kernel(CtaParams p) {
     while (n_in) {
       ecc = level;
       const uint32_t nd = level + 1;
-      const bool front = (level & 1) == 0;  // where this level's frontier sits
       uint32_t* cnt = &s_cnt[level % 3];
       if (threadIdx.x == 0) s_cnt[(level + 1) % 3] = 0;
       // Threads sweep the frontier; each expands one vertex's out-edges.
       for (uint32_t i = threadIdx.x; i < n_in; i += blockDim.x) {
-        const uint32_t u = front ? slab[i] : slab[V - 1 - i];
-        const uint32_t eb = __ldg(p.off + u), ee = __ldg(p.off + u + 1);
-        for (uint32_t e = eb; e < ee; ++e) {
-          const uint32_t v = __ldg(p.idx + e);
-          const uint32_t bit = 1u << (v & 31);
-          if constexpr (!GB) {
-            if (bits[v >> 5] & bit) continue;
+        uint32_t eb, ee;
+        q_get(level, i, &eb, &ee);
+        if constexpr (ER) {
+          // up to 4 edge records in flight before any visited check
+          for (uint32_t e = eb; e < ee; e += 4) {
+            uint4 r[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              if (e + k < ee) r[k] = __ldg(p.erec + e + k);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              if (e + k >= ee) break;
+              const uint32_t v = r[k].x;
+              const uint32_t bit = 1u << (v & 31);
+              if constexpr (!GB) {
+                if (bits[v >> 5] & bit) continue;
+              }
+              const uint32_t old = atomicOr(&bits[v >> 5], bit);
+              if (old & bit) continue;
+              if (row) row[v] = nd;
+              my_sum += nd;
+              ++my_cnt;
+              q_put(level + 1, atomicAdd(cnt, 1u), v, r[k].y, r[k].z);
+            }
           }
-          const uint32_t old = atomicOr(&bits[v >> 5], bit);
-          if (old & bit) continue;
-          if (row) row[v] = nd;
-          my_sum += nd;
-          ++my_cnt;
-          const uint32_t pos = atomicAdd(cnt, 1u);
-          if (front)
-            slab[V - 1 - pos] = v;
-          else
-            slab[pos] = v;
+        } else {
+          for (uint32_t e = eb; e < ee; ++e) {
+            const uint32_t v = __ldg(p.idx + e);
+            const uint32_t bit = 1u << (v & 31);
+            if constexpr (!GB) {
+              if (bits[v >> 5] & bit) continue;
+            }
+            const uint32_t old = atomicOr(&bits[v >> 5], bit);
+            if (old & bit) continue;
+            if (row) row[v] = nd;
+            my_sum += nd;
+            ++my_cnt;
+            q_put(level + 1, atomicAdd(cnt, 1u), v, 0, 0);
+          }
         }
       }
       __syncthreads();
@@ -127,6 +191,23 @@ __global__ void __launch_bounds__(CTA_THREADS) cta_bfs_kernel(CtaParams p) {
   }
 }
 
+// Edge records of a road-like graph: for every edge e = (u, v), {v, off[v],
+// off[v+1], 0}. One thread per vertex u.
+__global__ void edge_records_kernel(uint32_t V, const uint32_t* __restrict__ off,
+                                    const uint32_t* __restrict__ idx, uint4* __restrict__ erec) {
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < V; u += gridDim.x * blockDim.x) {
+    for (uint32_t e = off[u]; e < off[u + 1]; ++e) {
+      const uint32_t v = idx[e];
+      erec[e] = make_uint4(v, off[v], off[v + 1], 0u);
+    }
+  }
+}
+
+void launch_edge_records(uint32_t V, const uint32_t* off, const uint32_t* idx, uint4* erec,
+                         cudaStream_t s) {
+  edge_records_kernel<<<1024, 256, 0, s>>>(V, off, idx, erec);
+}
+
 size_t cta_max_vertices(int device) {
   int optin = 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
@@ -135,25 +216,54 @@ size_t cta_max_vertices(int device) {
   return ((size_t)optin - reserve) * 8;
 }
 
-bool cta_launch_shape(uint32_t V, int device, bool allow_global, CtaShape* out) {
-  int sms = 0;
+template <bool GB, bool ER>
+static int cta_occupancy(int block, size_t smem) {
+  cudaFuncSetAttribute(cta_bfs_kernel<GB, ER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<GB, ER>, block, smem);
+  return occ;
+}
+
+bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
+                      CtaShape* out) {
+  int sms = 0, optin = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   const size_t words = ((size_t)V + 31) / 32;
+  const size_t entry = edge_records ? 2 * sizeof(uint32_t) : sizeof(uint32_t);
   CtaShape sh{};
   sh.block = CTA_THREADS;
+  sh.edge_records = edge_records;
   int occ = 0;
+  // The queue halves get the shared memory left once the bitmaps of as many
+  // resident blocks as the threads allow (CTA_BLOCKS_PER_SM) have theirs: a
+  // many-source call is bound by how many BFSs run at once, so the queue
+  // never costs a resident block. A frontier beyond the halves continues in
+  // the global slab.
+  int per_sm = 0;
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+  const size_t bitmap = (size_t)V <= cta_max_vertices(device)
+                            ? (words + 1) / 2 * 2 * sizeof(uint32_t)  // 8-byte aligned end
+                            : 0;
+  const size_t slack = 2048;  // static shared variables + the driver's per-block reserve
+  const size_t fit = std::max<size_t>(1, (size_t)per_sm / (bitmap + slack));
+  const size_t blocks = std::min<size_t>(CTA_BLOCKS_PER_SM, fit);
+  const size_t budget = std::min<size_t>((size_t)per_sm / blocks, (size_t)optin) - slack;
+  const size_t room = budget > bitmap ? budget - bitmap : 0;
+  sh.qh = (uint32_t)std::min<size_t>(CTA_SMEM_QUEUE, room / (2 * entry) / 32 * 32);
   if ((size_t)V <= cta_max_vertices(device)) {
-    sh.smem = words * sizeof(uint32_t);
-    cudaFuncSetAttribute(cta_bfs_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh.smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<false>, sh.block,
-                                                  sh.smem);
+    sh.smem = bitmap + 2 * (size_t)sh.qh * entry;
+    occ = edge_records ? cta_occupancy<false, true>(sh.block, sh.smem)
+                       : cta_occupancy<false, false>(sh.block, sh.smem);
     if (occ < 1) return false;
     sh.grid = sms * occ;
   } else {
     if (!allow_global) return false;
     sh.global_bits = true;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<true>, sh.block, 0);
+    sh.smem = 2 * (size_t)sh.qh * entry;
+    occ = edge_records ? cta_occupancy<true, true>(sh.block, sh.smem)
+                       : cta_occupancy<true, false>(sh.block, sh.smem);
     if (occ < 1) return false;
     const size_t per_block = ((size_t)V + words) * sizeof(uint32_t);
     sh.grid = (int)std::max<size_t>(
@@ -163,11 +273,21 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, CtaShape* out) 
   return true;
 }
 
-void launch_cta(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s) {
-  if (sh.global_bits)
-    cta_bfs_kernel<true><<<grid, sh.block, 0, s>>>(p);
-  else
-    cta_bfs_kernel<false><<<grid, sh.block, sh.smem, s>>>(p);
+void launch_cta(const CtaParams& params, const CtaShape& sh, int grid, cudaStream_t s) {
+  CtaParams p = params;
+  p.qh = sh.qh;  // the dynamic shared memory holds exactly these queue halves
+  if (!sh.edge_records) p.erec = nullptr;
+  if (sh.global_bits) {
+    if (sh.edge_records)
+      cta_bfs_kernel<true, true><<<grid, sh.block, sh.smem, s>>>(p);
+    else
+      cta_bfs_kernel<true, false><<<grid, sh.block, sh.smem, s>>>(p);
+  } else {
+    if (sh.edge_records)
+      cta_bfs_kernel<false, true><<<grid, sh.block, sh.smem, s>>>(p);
+    else
+      cta_bfs_kernel<false, false><<<grid, sh.block, sh.smem, s>>>(p);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -232,7 +352,7 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
   }
   const uint32_t V = (uint32_t)num_vertices;
   CtaShape sh{};
-  if (!cta_launch_shape(V, device, /*allow_global=*/false, &sh))
+  if (!cta_launch_shape(V, device, /*allow_global=*/false, /*edge_records=*/false, &sh))
     return MSBFS_ERR_SCRATCH_TOO_SMALL;
   const size_t slabs = (NOALLOC_WORDS - NOALLOC_Q_OFF) / (size_t)V;
   const cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);

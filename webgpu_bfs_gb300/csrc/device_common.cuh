@@ -168,18 +168,26 @@ struct CtaParams {
   uint32_t* work;        // source cursor (zeroed before launch)
   SourceStats* stats;    // non-null: per-source reductions instead of rows
   uint32_t* gbits;       // global-bitmap mode: per resident block ceil(V/32) u32
+  uint32_t qh;           // frontier entries per shared-memory queue half (set at launch)
+  const uint4* erec;     // per edge {target, target's edge begin, end, 0}, or null
 };
 struct CtaShape {
   int grid = 0;           // resident blocks
   int block = 0;          // threads per block
-  size_t smem = 0;        // dynamic shared memory (the bitmap in shared mode)
+  size_t smem = 0;        // dynamic shared memory: bitmap (shared mode) + queue halves
+  uint32_t qh = 0;        // frontier entries per shared-memory queue half
   bool global_bits = false;
+  bool edge_records = false;
 };
 // Max V for the shared-memory visited bitmap; launch shape of the CTA kernel
-// (global-bitmap mode above that V when allow_global).
+// (global-bitmap mode above that V when allow_global; edge-range queue
+// entries when the graph has edge records).
 size_t cta_max_vertices(int device);
-bool cta_launch_shape(uint32_t V, int device, bool allow_global, CtaShape* out);
+bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
+                      CtaShape* out);
 void launch_cta(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s);
+void launch_edge_records(uint32_t V, const uint32_t* off, const uint32_t* idx, uint4* erec,
+                         cudaStream_t s);
 
 void launch_traversed_edges(uint32_t V, const uint32_t* off, const uint32_t* dist,
                             uint32_t num_sources, unsigned long long* out, cudaStream_t s);

@@ -57,6 +57,8 @@ struct msbfs_graph {
   // Bottom-up work order: vertices with 0 < in-degree <= split, ascending ids.
   uint32_t n_order = 0;
   uint32_t* order = nullptr;
+  // Road-like graphs: per edge {target, target's edge begin, end, 0}.
+  uint4* erec = nullptr;
 };
 
 namespace {
@@ -124,7 +126,10 @@ struct msbfs_engine {
   uint32_t alpha = 14;
   uint32_t beta = 24;
   uint32_t seg = 64;
-  uint32_t heavy = 32;
+#ifndef MSBFS_HEAVY
+#define MSBFS_HEAVY 32
+#endif
+  uint32_t heavy = MSBFS_HEAVY;  // in-degree from which a whole warp scans a vertex
 #ifndef MSBFS_SPLIT
 #define MSBFS_SPLIT 256
 #endif
@@ -479,11 +484,13 @@ int validate_call(msbfs_engine* eng, const msbfs_graph* g, const uint32_t* sourc
   return MSBFS_OK;
 }
 
+// The router's road test (engine.rs:157-198): low degree, sparse.
+bool is_road_like(const msbfs_graph* g) { return g->max_deg <= 8 && g->E <= 4 * g->V; }
+
 int resolve_method(const msbfs_graph* g, int method, size_t S) {
   if (method == MSBFS_METHOD_AUTO) {
     if (g->V == 0 || S == 0) return MSBFS_METHOD_NAIVE_SEQUENTIAL;
-    const bool road = g->max_deg <= 8 && g->E <= 4 * g->V;
-    if (road) return MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS;
+    if (is_road_like(g)) return MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS;
     if (g->max_deg >= 128) return MSBFS_METHOD_INDIRECT_SPARSE_QUEUE_PUSH;
     if (S >= 64) return MSBFS_METHOD_MULTI_WORD_BIT_PARALLEL;
     if (S >= 32) return MSBFS_METHOD_BIT_PARALLEL_64;
@@ -506,7 +513,8 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   uint32_t path = method_path(m);
   if (reach_dev && path == MSBFS_PATH_CTA) path = MSBFS_PATH_HYBRID;
   CtaShape cta{};
-  if (path == MSBFS_PATH_CTA && !cta_launch_shape((uint32_t)g->V, eng->device, true, &cta))
+  if (path == MSBFS_PATH_CTA &&
+      !cta_launch_shape((uint32_t)g->V, eng->device, true, g->erec != nullptr, &cta))
     path = MSBFS_PATH_HYBRID;
   const int cta_grid = std::max(1, (int)((uint64_t)cta.grid * eng->sm_share / 100));
   if (!g->sym && path != MSBFS_PATH_CTA && !g->coff)
@@ -541,6 +549,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     cp.work = eng->d_work;
     cp.stats = stats_dev;
     cp.gbits = cta.global_bits ? eng->d_cta_bits : nullptr;
+    cp.erec = g->erec;
     launch_cta(cp, cta, blocks, eng->stream);
     CK(cudaGetLastError());
     eng->last.passes = 1;
@@ -764,6 +773,15 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
     if (!order.empty())
       CK(cudaMemcpy(g->order, order.data(), order.size() * 4, cudaMemcpyHostToDevice));
   }
+  // Road-like graphs (the ones the router sends to the CTA path) get edge
+  // records, 16 bytes per edge, so a CTA-path level costs one dependent L2
+  // round trip instead of three.
+  if (is_road_like(g.get()) && E > 0) {
+    CK(cudaMalloc((void**)&g->erec, E * sizeof(uint4)));
+    launch_edge_records((uint32_t)V, g->off, g->idx, g->erec, eng->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(eng->stream));
+  }
   *out = g.release();
   return MSBFS_OK;
 }
@@ -791,6 +809,7 @@ void free_graph(msbfs_graph* g) {
   cudaFree(g->idx);
   cudaFree(g->hchunks);
   cudaFree(g->order);
+  cudaFree(g->erec);
   delete g;
 }
 

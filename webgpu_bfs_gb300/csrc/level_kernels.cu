@@ -39,7 +39,6 @@ constexpr int BQ_CAP = 2048;  // discovered vertices staged per block
 #define MSBFS_LEVEL_MIN_BLOCKS 6
 #endif
 constexpr int CH = MSBFS_PULL_CH;  // in-neighbours gathered per chunk
-constexpr int MAT_KC = 8;     // words per materialise chunk
 constexpr int MAT_BLOCK = 256;
 constexpr uint32_t FULL = 0xffffffffu;
 constexpr uint32_t DIST_MAX = 0xffffffffu;
@@ -258,8 +257,10 @@ __device__ __forceinline__ void record_level(const LevelParams& p, uint32_t v, u
   }
 }
 
+// Per-thread work counts of one level (32-bit: a thread's share of a level
+// stays far below 2^32; they are widened when the block reduces them).
 struct LevelCounters {
-  unsigned long long active = 0, edges = 0, newv = 0, pairs = 0, rows = 0;
+  uint32_t active = 0, edges = 0, newv = 0, pairs = 0, rows = 0;
 };
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -319,7 +320,13 @@ __device__ __forceinline__ bool in_frontier(const uint32_t* fb, uint32_t u) {
   return !fb || ((__ldg(fb + (u >> 5)) >> (u & 31)) & 1u);
 }
 
-constexpr uint32_t TILE_BATCH = 16;  // vertex tiles claimed per cursor bump
+// Vertex tiles a warp claims per cursor bump: small batches even out the end
+// of a level (R-MAT scale 22, S=512, bottom-up time: 4 tiles 8% and 8 tiles
+// 6% below 16; 32 tiles 15% above).
+#ifndef MSBFS_TILE_BATCH
+#define MSBFS_TILE_BATCH 4
+#endif
+constexpr uint32_t TILE_BATCH = MSBFS_TILE_BATCH;
 
 // Bottom-up step over all vertices, in two parts.
 // (1) Sliced vertices (in-degree > split): each warp takes one slice of one
@@ -942,10 +949,6 @@ __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint
   }
 }
 
-// Turns visited words + level planes into the source-major u32 distance rows
-// (or copies the visited words out as a reachability bitmask) and zeroes the
-// words it read, so the next pass starts from clean buffers. Warps take
-// (vertex tile, word) items independently: no shared memory, no barriers.
 // Per-source reductions straight from the visited words and level planes
 // (no S*V matrix): a warp item is word c of 1024 consecutive vertices, lane j
 // accumulates source 32c+j, and each lane loads one vertex's words which the
@@ -1012,6 +1015,11 @@ __device__ void reduce_sources(const LevelParams& p, uint32_t P, uint32_t npu, b
   }
 }
 
+// Turns visited words + level planes into the source-major u32 distance rows
+// (or copies the visited words out as a reachability bitmask, or reduces them
+// to per-source statistics) and zeroes the words it read, so the next pass
+// starts from clean buffers. Warps take (vertex tile, word) items
+// independently: no shared memory, no barriers.
 template <int W>
 __global__ void __launch_bounds__(MAT_BLOCK, 4) materialize_kernel(LevelParams p) {
   const PassDesc* dsc = p.desc;
