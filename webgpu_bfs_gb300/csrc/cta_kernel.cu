@@ -23,7 +23,14 @@ namespace msbfs {
 
 constexpr uint32_t CTA_DIST_MAX = 0xffffffffu;
 constexpr int CTA_THREADS = 512;
-constexpr int CTA_BLOCKS_PER_SM = 4;  // 2,048 threads: every thread slot of an SM
+// Two register budgets per kernel: MINB = 3 resident blocks per SM (40
+// registers: 4 edge records in flight, the shortest level latency) and MINB =
+// 4 (32 registers, 2 records in flight, every thread slot of the SM). A call
+// with more sources than 3 blocks per SM can hold gets the 4-block form:
+// many-source calls are bound by how many BFSs run at once, single ones by
+// the per-level latency chain.
+constexpr int CTA_MINB_LATENCY = 3;
+constexpr int CTA_MINB_THROUGHPUT = 4;
 // Global-bitmap mode keeps its per-block scratch (queue slab + bitmap) within
 // this many bytes by shrinking the grid.
 constexpr size_t CTA_GLOBAL_SCRATCH_BYTES = 4ull << 30;
@@ -49,8 +56,9 @@ constexpr uint32_t CTA_SMEM_QUEUE = 4096;
 // Counters: level L appends through s_cnt[L % 3]; thread 0 clears
 // s_cnt[(L+1) % 3] during level L (last read right after the barrier of
 // level L-2), so a level needs one block barrier.
-template <bool GB, bool ER>
-__global__ void __launch_bounds__(CTA_THREADS, CTA_BLOCKS_PER_SM) cta_bfs_kernel(CtaParams p) {
+template <bool GB, bool ER, int MINB>
+__global__ void __launch_bounds__(CTA_THREADS, MINB) cta_bfs_kernel(CtaParams p) {
+  constexpr int CTA_ER_BATCH = MINB >= CTA_MINB_THROUGHPUT ? 2 : 4;
   extern __shared__ __align__(16) uint32_t smem_dyn[];
   __shared__ uint32_t s_src_idx;
   __shared__ uint32_t s_cnt[3];
@@ -125,14 +133,16 @@ __global__ void __launch_bounds__(CTA_THREADS, CTA_BLOCKS_PER_SM) cta_bfs_kernel
         uint32_t eb, ee;
         q_get(level, i, &eb, &ee);
         if constexpr (ER) {
-          // up to 4 edge records in flight before any visited check
-          for (uint32_t e = eb; e < ee; e += 4) {
-            uint4 r[4];
+          // CTA_ER_BATCH edge records in flight before any visited check
+          // (road vertices have ~2 edges; more would cost registers, and so
+          // resident blocks, for little gain)
+          for (uint32_t e = eb; e < ee; e += CTA_ER_BATCH) {
+            uint4 r[CTA_ER_BATCH];
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
+            for (int k = 0; k < CTA_ER_BATCH; ++k)
               if (e + k < ee) r[k] = __ldg(p.erec + e + k);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < CTA_ER_BATCH; ++k) {
               if (e + k >= ee) break;
               const uint32_t v = r[k].x;
               const uint32_t bit = 1u << (v & 31);
@@ -216,61 +226,72 @@ size_t cta_max_vertices(int device) {
   return ((size_t)optin - reserve) * 8;
 }
 
-template <bool GB, bool ER>
+template <bool GB, bool ER, int MINB>
 static int cta_occupancy(int block, size_t smem) {
-  cudaFuncSetAttribute(cta_bfs_kernel<GB, ER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(cta_bfs_kernel<GB, ER, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<GB, ER>, block, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<GB, ER, MINB>, block, smem);
   return occ;
 }
 
+template <bool GB, bool ER>
+static int cta_occupancy(int minb, int block, size_t smem) {
+  return minb >= CTA_MINB_THROUGHPUT ? cta_occupancy<GB, ER, CTA_MINB_THROUGHPUT>(block, smem)
+                                     : cta_occupancy<GB, ER, CTA_MINB_LATENCY>(block, smem);
+}
+
 bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
-                      CtaShape* out) {
-  int sms = 0, optin = 0;
+                      size_t num_sources, CtaShape* out) {
+  int sms = 0, optin = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
   const size_t words = ((size_t)V + 31) / 32;
   const size_t entry = edge_records ? 2 * sizeof(uint32_t) : sizeof(uint32_t);
+  const bool shared_bits = (size_t)V <= cta_max_vertices(device);
+  if (!shared_bits && !allow_global) return false;
   CtaShape sh{};
   sh.block = CTA_THREADS;
   sh.edge_records = edge_records;
-  int occ = 0;
-  // The queue halves get the shared memory left once the bitmaps of as many
-  // resident blocks as the threads allow (CTA_BLOCKS_PER_SM) have theirs: a
-  // many-source call is bound by how many BFSs run at once, so the queue
-  // never costs a resident block. A frontier beyond the halves continues in
-  // the global slab.
-  int per_sm = 0;
-  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
-  const size_t bitmap = (size_t)V <= cta_max_vertices(device)
-                            ? (words + 1) / 2 * 2 * sizeof(uint32_t)  // 8-byte aligned end
-                            : 0;
+  sh.global_bits = !shared_bits;
+  sh.minb = (shared_bits && num_sources > (size_t)sms * CTA_MINB_LATENCY) ? CTA_MINB_THROUGHPUT
+                                                                          : CTA_MINB_LATENCY;
+  // The queue halves get the shared memory left once the bitmaps of minb
+  // resident blocks have theirs, so the queue never costs a resident block.
+  // A frontier beyond the halves continues in the global slab.
+  const size_t bitmap = shared_bits ? (words + 1) / 2 * 2 * sizeof(uint32_t) : 0;  // 8-byte end
   const size_t slack = 2048;  // static shared variables + the driver's per-block reserve
   const size_t fit = std::max<size_t>(1, (size_t)per_sm / (bitmap + slack));
-  const size_t blocks = std::min<size_t>(CTA_BLOCKS_PER_SM, fit);
+  const size_t blocks = std::min<size_t>((size_t)sh.minb, fit);
   const size_t budget = std::min<size_t>((size_t)per_sm / blocks, (size_t)optin) - slack;
   const size_t room = budget > bitmap ? budget - bitmap : 0;
   sh.qh = (uint32_t)std::min<size_t>(CTA_SMEM_QUEUE, room / (2 * entry) / 32 * 32);
-  if ((size_t)V <= cta_max_vertices(device)) {
-    sh.smem = bitmap + 2 * (size_t)sh.qh * entry;
-    occ = edge_records ? cta_occupancy<false, true>(sh.block, sh.smem)
-                       : cta_occupancy<false, false>(sh.block, sh.smem);
-    if (occ < 1) return false;
-    sh.grid = sms * occ;
-  } else {
-    if (!allow_global) return false;
-    sh.global_bits = true;
-    sh.smem = 2 * (size_t)sh.qh * entry;
-    occ = edge_records ? cta_occupancy<true, true>(sh.block, sh.smem)
-                       : cta_occupancy<true, false>(sh.block, sh.smem);
-    if (occ < 1) return false;
+  sh.smem = bitmap + 2 * (size_t)sh.qh * entry;
+  int occ;
+  if (shared_bits)
+    occ = edge_records ? cta_occupancy<false, true>(sh.minb, sh.block, sh.smem)
+                       : cta_occupancy<false, false>(sh.minb, sh.block, sh.smem);
+  else
+    occ = edge_records ? cta_occupancy<true, true>(sh.minb, sh.block, sh.smem)
+                       : cta_occupancy<true, false>(sh.minb, sh.block, sh.smem);
+  if (occ < 1) return false;
+  sh.grid = sms * occ;
+  if (!shared_bits) {
     const size_t per_block = ((size_t)V + words) * sizeof(uint32_t);
     sh.grid = (int)std::max<size_t>(
-        1, std::min<size_t>((size_t)sms * occ, CTA_GLOBAL_SCRATCH_BYTES / per_block));
+        1, std::min<size_t>((size_t)sh.grid, CTA_GLOBAL_SCRATCH_BYTES / per_block));
   }
   *out = sh;
   return true;
+}
+
+template <bool GB, bool ER>
+static void launch_cta_t(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s) {
+  if (sh.minb >= CTA_MINB_THROUGHPUT)
+    cta_bfs_kernel<GB, ER, CTA_MINB_THROUGHPUT><<<grid, sh.block, sh.smem, s>>>(p);
+  else
+    cta_bfs_kernel<GB, ER, CTA_MINB_LATENCY><<<grid, sh.block, sh.smem, s>>>(p);
 }
 
 void launch_cta(const CtaParams& params, const CtaShape& sh, int grid, cudaStream_t s) {
@@ -279,14 +300,14 @@ void launch_cta(const CtaParams& params, const CtaShape& sh, int grid, cudaStrea
   if (!sh.edge_records) p.erec = nullptr;
   if (sh.global_bits) {
     if (sh.edge_records)
-      cta_bfs_kernel<true, true><<<grid, sh.block, sh.smem, s>>>(p);
+      launch_cta_t<true, true>(p, sh, grid, s);
     else
-      cta_bfs_kernel<true, false><<<grid, sh.block, sh.smem, s>>>(p);
+      launch_cta_t<true, false>(p, sh, grid, s);
   } else {
     if (sh.edge_records)
-      cta_bfs_kernel<false, true><<<grid, sh.block, sh.smem, s>>>(p);
+      launch_cta_t<false, true>(p, sh, grid, s);
     else
-      cta_bfs_kernel<false, false><<<grid, sh.block, sh.smem, s>>>(p);
+      launch_cta_t<false, false>(p, sh, grid, s);
   }
 }
 
@@ -352,7 +373,8 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
   }
   const uint32_t V = (uint32_t)num_vertices;
   CtaShape sh{};
-  if (!cta_launch_shape(V, device, /*allow_global=*/false, /*edge_records=*/false, &sh))
+  if (!cta_launch_shape(V, device, /*allow_global=*/false, /*edge_records=*/false, num_sources,
+                        &sh))
     return MSBFS_ERR_SCRATCH_TOO_SMALL;
   const size_t slabs = (NOALLOC_WORDS - NOALLOC_Q_OFF) / (size_t)V;
   const cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);

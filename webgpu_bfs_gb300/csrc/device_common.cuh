@@ -133,6 +133,11 @@ struct LevelParams {
   const HeavyChunk* hchunks;
   uint32_t* hcand;    // [n_heavy][W] candidate words of sliced vertices
   uint32_t* hcount;   // [n_heavy] slices finished this level
+  // Bit ci: the vertex of slice ci may still need lanes. Set at pass start,
+  // cleared for good once the slice finds none needed (a vertex's needed
+  // lanes only shrink: visited lanes grow, live lanes die).
+  uint32_t* hlive;
+  uint32_t hlive_words;
   uint32_t bits_div;  // bitmap check when the frontier holds < V / bits_div vertices
   uint32_t n_order;
   const uint32_t* order;  // vertices with 0 < in-degree <= split (work order)
@@ -176,15 +181,16 @@ struct CtaShape {
   int block = 0;          // threads per block
   size_t smem = 0;        // dynamic shared memory: bitmap (shared mode) + queue halves
   uint32_t qh = 0;        // frontier entries per shared-memory queue half
+  int minb = 3;           // register budget: resident blocks per SM it is built for
   bool global_bits = false;
   bool edge_records = false;
 };
 // Max V for the shared-memory visited bitmap; launch shape of the CTA kernel
-// (global-bitmap mode above that V when allow_global; edge-range queue
-// entries when the graph has edge records).
+// for a call of num_sources sources (global-bitmap mode above that V when
+// allow_global; edge-range queue entries when the graph has edge records).
 size_t cta_max_vertices(int device);
 bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
-                      CtaShape* out);
+                      size_t num_sources, CtaShape* out);
 void launch_cta(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s);
 void launch_edge_records(uint32_t V, const uint32_t* off, const uint32_t* idx, uint4* erec,
                          cudaStream_t s);

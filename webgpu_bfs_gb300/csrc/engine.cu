@@ -242,6 +242,15 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w) {
   m3.height = 1;
   m3.pitch = m3.width * 4;
   CK(cudaGraphAddMemsetNode(&n_mfb, g, nullptr, 0, &m3));
+  cudaGraphNode_t n_mhl;
+  cudaMemsetParams m4{};
+  m4.dst = w->p.hlive;
+  m4.value = 0xFFFFFFFFu;
+  m4.elementSize = 4;
+  m4.width = std::max(w->p.hlive_words, 1u);
+  m4.height = 1;
+  m4.pitch = m4.width * 4;
+  CK(cudaGraphAddMemsetNode(&n_mhl, g, nullptr, 0, &m4));
 
   void* args_p[] = {&w->p};
   cudaKernelNodeParams ki{};
@@ -250,8 +259,8 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w) {
   ki.blockDim = dim3(256);
   ki.sharedMemBytes = 0;
   ki.kernelParams = args_p;
-  cudaGraphNode_t deps_init[3] = {n_mctl, n_mst, n_mfb};
-  CK(cudaGraphAddKernelNode(&n_init, g, deps_init, 3, &ki));
+  cudaGraphNode_t deps_init[4] = {n_mctl, n_mst, n_mfb, n_mhl};
+  CK(cudaGraphAddKernelNode(&n_init, g, deps_init, 4, &ki));
 
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
@@ -371,6 +380,9 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   p.hcand = (uint32_t*)ptr;
   if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)g->n_heavy * 4))) return rc;
   p.hcount = (uint32_t*)ptr;
+  p.hlive_words = (g->n_hchunks + 31) / 32;
+  if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)std::max(p.hlive_words, 1u) * 4))) return rc;
+  p.hlive = (uint32_t*)ptr;
   if (!eng->host_loop) {
     rc = build_graph_exec(eng, w.get());
     if (rc) {
@@ -404,6 +416,8 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
   CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
   CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
   CK(cudaMemsetAsync(w->p.fbits[0], 0, 3 * ((w->p.V + 31) / 32) * sizeof(uint32_t), eng->stream));
+  if (w->p.hlive_words)
+    CK(cudaMemsetAsync(w->p.hlive, 0xFF, w->p.hlive_words * sizeof(uint32_t), eng->stream));
   launch_init(w->p, eng->stream);
   LevelCtl probe{};
   ms->clear();
@@ -437,6 +451,8 @@ int run_pass_host_loop(msbfs_engine* eng, Workspace* w) {
   CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
   CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
   CK(cudaMemsetAsync(w->p.fbits[0], 0, 3 * ((w->p.V + 31) / 32) * sizeof(uint32_t), eng->stream));
+  if (w->p.hlive_words)
+    CK(cudaMemsetAsync(w->p.hlive, 0xFF, w->p.hlive_words * sizeof(uint32_t), eng->stream));
   launch_init(w->p, eng->stream);
   LevelCtl probe{};
   for (uint64_t launched = 0;;) {
@@ -514,7 +530,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   if (reach_dev && path == MSBFS_PATH_CTA) path = MSBFS_PATH_HYBRID;
   CtaShape cta{};
   if (path == MSBFS_PATH_CTA &&
-      !cta_launch_shape((uint32_t)g->V, eng->device, true, g->erec != nullptr, &cta))
+      !cta_launch_shape((uint32_t)g->V, eng->device, true, g->erec != nullptr, S, &cta))
     path = MSBFS_PATH_HYBRID;
   const int cta_grid = std::max(1, (int)((uint64_t)cta.grid * eng->sm_share / 100));
   if (!g->sym && path != MSBFS_PATH_CTA && !g->coff)

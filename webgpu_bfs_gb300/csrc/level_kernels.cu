@@ -358,8 +358,17 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
   const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
 
-  // ---- (1) sliced high in-degree vertices
-  for (uint32_t ci = warp_g; ci < p.n_hchunks; ci += nwarps) {
+  // ---- (1) sliced high in-degree vertices. A warp takes its slices 32 at a
+  // time and first tests their bits in p.hlive, so slices whose vertex needs
+  // no lane any more (cleared below, for the rest of the pass) cost one bit
+  // test instead of a chain of dependent loads.
+  for (uint32_t cb = warp_g; cb < p.n_hchunks; cb += 32 * nwarps) {
+    const uint32_t mine = cb + lane * nwarps;
+    const bool live = mine < p.n_hchunks && ((p.hlive[mine >> 5] >> (mine & 31)) & 1u);
+    uint32_t todo = __ballot_sync(FULL, live);
+   while (todo) {
+    const uint32_t ci = cb + (__ffs(todo) - 1) * nwarps;
+    todo &= todo - 1;
     const HeavyChunk hk = p.hchunks[ci];
     const uint32_t v = hk.v;
     const uint32_t vb = __ldg(in_off + v);
@@ -378,7 +387,10 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     }
     // Every slice of v sees the same `needed` (only the committing slice
     // writes v's visited row, after all slices arrived).
-    if (!__any_sync(FULL, any_bits<VEC>(needed))) continue;
+    if (!__any_sync(FULL, any_bits<VEC>(needed))) {
+      if (lane == 0) atomicAnd(&p.hlive[ci >> 5], ~(1u << (ci & 31)));
+      continue;
+    }
     if (hk.j == 0 && lane == 0) cnt.active += 1;
     if (!__all_sync(FULL, sat)) {
       // Each round the warp gathers GPW*CH in-neighbours; the ids of the next
@@ -453,6 +465,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         if (lane == 0) p.hcount[hk.h] = 0;
       }
     }
+   }
   }
 
   // ---- (2) all other vertices with in-edges, in the graph's work order
