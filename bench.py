@@ -335,6 +335,8 @@ def run_ours(args, spec):
     tedges = eng.traversed_edges_device(g, out.data_ptr(), S)
     gteps = tedges * args.steps / (max_ms / 1000.0) / 1e9 * world
 
+    # per pass: init, one level kernel per level, materialise, cleanup; the
+    # CTA path is one launch
     launches_per_step = (st["levels"] + 3) * st["passes"] if st["path"] != 4 else 1
 
     # ---- roofline of the level kernel: per-launch CUDA events in a host-driven

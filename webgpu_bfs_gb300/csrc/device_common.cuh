@@ -41,6 +41,7 @@ struct LevelRec {
 };
 
 constexpr uint32_t LOG_CAP = 4096;
+constexpr uint32_t WORK_STRIPES = 16;
 
 struct LevelCtl {
   uint32_t level;      // frontier level L being expanded
@@ -62,8 +63,12 @@ struct LevelCtl {
   unsigned long long c_pairs;
   unsigned long long c_rows;
   unsigned long long t_start;    // min %globaltimer over the level's blocks
-  uint32_t work;                 // vertex-tile cursor of the running bottom-up step
   uint32_t use_bits;             // bottom-up step checks frontier bitmaps first
+  // Vertex-tile cursors of the running bottom-up step: the work list is cut
+  // into WORK_STRIPES contiguous stripes, each with its own cursor on its own
+  // 128-byte line, so the claims of a level spread over several L2 slices
+  // instead of queueing on one address.
+  alignas(128) uint32_t work[WORK_STRIPES][32];
 
   // Source lanes whose frontier is non-empty: lanes[L & 1] for the level being
   // expanded, lanes[(L + 1) & 1] collects the lanes that gain vertices. A lane

@@ -474,14 +474,26 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
   // claimed dynamically: work concentrates at some ids (R-MAT puts its hubs
   // first) and a static split would leave most warps idle behind a few.
   const uint32_t ntiles = (p.n_order + GPW - 1) / GPW;
+  const uint32_t per_stripe = (ntiles + WORK_STRIPES - 1) / WORK_STRIPES;
+  uint32_t stripe = warp_g % WORK_STRIPES, exhausted = 0;
   uint32_t tile = 0, tile_end = 0;
   for (;;) {
     if (tile == tile_end) {
-      uint32_t t0 = 0;
-      if (lane == 0) t0 = atomicAdd(&p.ctl->work, TILE_BATCH);
-      tile = __shfl_sync(FULL, t0, 0);
-      if (tile >= ntiles) break;
-      tile_end = min(tile + TILE_BATCH, ntiles);
+      // Claim from the warp's stripe; move to the next once it runs dry.
+      while (exhausted < WORK_STRIPES) {
+        const uint32_t sb = stripe * per_stripe, se = min(sb + per_stripe, ntiles);
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = sb < se ? sb + atomicAdd(&p.ctl->work[stripe][0], TILE_BATCH) : se;
+        t0 = __shfl_sync(FULL, t0, 0);
+        if (t0 < se) {
+          tile = t0;
+          tile_end = min(t0 + TILE_BATCH, se);
+          break;
+        }
+        ++exhausted;
+        stripe = (stripe + 1) % WORK_STRIPES;
+      }
+      if (tile == tile_end) break;  // every stripe is done
     }
     const uint32_t oi = tile * GPW + gid;
     ++tile;
@@ -761,7 +773,7 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
   c->dir = nd;
   c->level = L + 1;
   c->done_blocks = 0;
-  c->work = 0;
+  for (uint32_t k = 0; k < WORK_STRIPES; ++k) c->work[k][0] = 0;
   c->use_bits = (p.bits_div && (unsigned long long)n_next * p.bits_div < p.V) ? 1u : 0u;
   __threadfence();
   if (h) cudaGraphSetConditional(h, 1);
