@@ -145,7 +145,7 @@ struct LevelParams {
   uint32_t hlive_words;
   uint32_t bits_div;  // bitmap check when the frontier holds < V / bits_div vertices
   uint32_t n_order;
-  const uint32_t* order;  // vertices with 0 < in-degree <= split (work order)
+  const uint4* order;  // {v, in-edge begin, end, 0} for 0 < in-degree <= split (work order)
 };
 
 // Launch helpers implemented in level_kernels.cu / cta_kernel.cu.

@@ -56,7 +56,7 @@ struct msbfs_graph {
   HeavyChunk* hchunks = nullptr;
   // Bottom-up work order: vertices with 0 < in-degree <= split, ascending ids.
   uint32_t n_order = 0;
-  uint32_t* order = nullptr;
+  uint4* order = nullptr;  // {vertex, in-edge begin, in-edge end, 0}
   // Road-like graphs: per edge {target, target's edge begin, end, 0}.
   uint4* erec = nullptr;
 };
@@ -785,9 +785,16 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
                          deg_desc);
     }
     g->n_order = (uint32_t)order.size();
-    CK(cudaMalloc((void**)&g->order, std::max<size_t>(order.size(), 1) * 4));
-    if (!order.empty())
-      CK(cudaMemcpy(g->order, order.data(), order.size() * 4, cudaMemcpyHostToDevice));
+    // Each entry carries the vertex and its in-edge range, so a bottom-up
+    // step starts a vertex's scan one dependent load earlier.
+    std::vector<uint4> ent(order.size());
+    for (size_t i = 0; i < order.size(); ++i) {
+      const uint32_t v = order[i];
+      ent[i] = make_uint4(v, t.off[v], t.off[v + 1], 0u);
+    }
+    CK(cudaMalloc((void**)&g->order, std::max<size_t>(ent.size(), 1) * sizeof(uint4)));
+    if (!ent.empty())
+      CK(cudaMemcpy(g->order, ent.data(), ent.size() * sizeof(uint4), cudaMemcpyHostToDevice));
   }
   // Road-like graphs (the ones the router sends to the CTA path) get edge
   // records, 16 bytes per edge, so a CTA-path level costs one dependent L2

@@ -328,6 +328,13 @@ __device__ __forceinline__ bool in_frontier(const uint32_t* fb, uint32_t u) {
 #endif
 constexpr uint32_t TILE_BATCH = MSBFS_TILE_BATCH;
 
+// In-neighbour id as gathered: FULL when absent or, with a frontier bitmap,
+// outside the frontier (so its row is not loaded). The lane holding an id
+// tests it once for its whole group before the id is shuffled out.
+__device__ __forceinline__ uint32_t gather_id(const uint32_t* fb, uint32_t u) {
+  return (u != FULL && in_frontier(fb, u)) ? u : FULL;
+}
+
 // Bottom-up step over all vertices, in two parts.
 // (1) Sliced vertices (in-degree > split): each warp takes one slice of one
 //     vertex's in-edges, ORs the in-neighbours' frontier rows (every group of
@@ -408,11 +415,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         if (lig == 0 && e0 < end) cnt.edges += min((uint32_t)CH, end - e0);
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
+          const uint32_t mine = gather_id(fb, ids[0]);
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, ids[0], gbase + j);
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, mine, gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = ids[j];
+          for (int j = 0; j < CH; ++j) u[j] = gather_id(fb, ids[j]);
         }
 #pragma unroll
         for (int j = 0; j < NI; ++j) {
@@ -421,7 +429,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         }
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (u[j] != FULL && in_frontier(fb, u[j])) {
+          if (u[j] != FULL) {
             cnt.rows += 1;
             Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
 #pragma unroll
@@ -499,9 +507,10 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     ++tile;
     uint32_t v = 0, beg = 0, end = 0;
     if (oi < p.n_order) {
-      v = __ldg(p.order + oi);
-      beg = __ldg(in_off + v);
-      end = __ldg(in_off + v + 1);
+      const uint4 ent = __ldg(p.order + oi);
+      v = ent.x;
+      beg = ent.y;
+      end = ent.z;
     }
     Words<VEC> needed, visw, cand;
 #pragma unroll
@@ -529,11 +538,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
       for (uint32_t e0 = beg; e0 < end; e0 += CH) {
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
+          const uint32_t mine = gather_id(fb, ids[0]);
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(gmask, ids[0], gbase + j);
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(gmask, mine, gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = ids[j];
+          for (int j = 0; j < CH; ++j) u[j] = gather_id(fb, ids[j]);
         }
 #pragma unroll
         for (int j = 0; j < NI; ++j) {
@@ -545,7 +555,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         // A lane whose own words are covered skips its 16-byte pieces.
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (!lane_sat && u[j] != FULL && in_frontier(fb, u[j])) {
+          if (!lane_sat && u[j] != FULL) {
             cnt.rows += 1;
             f[j] = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
           } else {
@@ -591,11 +601,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         if (lig == 0 && e0 < hend) cnt.edges += min((uint32_t)CH, hend - e0);
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
+          const uint32_t mine = gather_id(fb, ids[0]);
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, ids[0], gbase + j);
+          for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, mine, gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = ids[j];
+          for (int j = 0; j < CH; ++j) u[j] = gather_id(fb, ids[j]);
         }
 #pragma unroll
         for (int j = 0; j < NI; ++j) {
@@ -604,7 +615,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         }
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
-          if (u[j] != FULL && in_frontier(fb, u[j])) {
+          if (u[j] != FULL) {
             cnt.rows += 1;
             Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
 #pragma unroll
@@ -887,36 +898,61 @@ __global__ void init_kernel(LevelParams p) {
 __device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __clz(x) : 0; }
 
 // Materialisation: a work item is word c (sources 32c .. 32c+31 of the
-// pass) of MAT_TV consecutive vertices, 4 per lane, so each distance row is
-// written with 16-byte stores (one vertex per lane with 4-byte stores
-// measured 1.6x slower on R-MAT scale 22, S=512, despite more resident warps).
-constexpr int MAT_TV = 128;  // vertices per work item (4 per lane)
+// pass) of MAT_TV consecutive vertices, MAT_VPL per lane, so each distance
+// row is written with 8- or 16-byte stores. On R-MAT scale 22, S=512: 2
+// vertices per lane (8-byte stores, 40 registers, 6 blocks per SM) 3.9 ms;
+// 4 per lane (16-byte stores, 64 registers, 4 blocks) 5.4 ms; 1 per lane
+// (4-byte stores) 8.7 ms.
+#ifndef MSBFS_MAT_VPL
+#define MSBFS_MAT_VPL 2
+#endif
+constexpr int MAT_VPL = MSBFS_MAT_VPL;  // vertices per lane: 2 or 4
+constexpr int MAT_TV = 32 * MAT_VPL;    // vertices per work item
 constexpr int MAT_NPMAX = 8;
+constexpr int MAT_MIN_BLOCKS = MAT_VPL == 4 ? 4 : 6;
 
-// One work item: word c of the 128 vertices v0 .. v0+127, i.e. the 32 sources
-// 32c .. 32c+31 of this pass. Lane l owns vertices v0+4l .. v0+4l+3: it loads
-// their visited / overflow / plane words (strided by W words; the warps of a
-// block take consecutive words of the same vertices, so the 32-byte sectors
-// are shared through L1), zeroes them, and writes the 32 distance rows as
-// 512-byte contiguous segments (one 16-byte store per lane per row). NPU
+template <int N>
+struct MatVec;
+template <>
+struct MatVec<4> {
+  static __device__ __forceinline__ void store(uint32_t* row, const uint32_t (&d)[4]) {
+    *reinterpret_cast<uint4*>(row) = make_uint4(d[0], d[1], d[2], d[3]);
+  }
+};
+template <>
+struct MatVec<2> {
+  static __device__ __forceinline__ void store(uint32_t* row, const uint32_t (&d)[2]) {
+    *reinterpret_cast<uint2*>(row) = make_uint2(d[0], d[1]);
+  }
+};
+
+// One work item: word c of the MAT_TV vertices from v0, i.e. the 32 sources
+// 32c .. 32c+31 of this pass. Lane l owns vertices v0 + MAT_VPL*l onwards: it
+// loads their visited / overflow / plane words (strided by W words; the warps
+// of a block take consecutive words of the same vertices, so the 32-byte
+// sectors are shared through L1), zeroes them, and writes the 32 distance
+// rows as contiguous segments (one MAT_VPL-word store per lane per row). NPU
 // (planes in use) is a template argument so the plane words stay in
 // registers.
 template <int NPU>
 __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint32_t c,
                                          uint32_t lane, uint32_t P, bool use_ovf,
                                          bool vec_ok) {
+  constexpr int T = MAT_VPL;
   const uint32_t W = p.W;
   const uint32_t V = p.V;
   const size_t VW = (size_t)V * W;
-  const uint32_t vl = v0 + 4 * lane;
-  uint32_t xs[4] = {0, 0, 0, 0}, ov[4] = {0, 0, 0, 0};
-  uint32_t pl[NPU > 0 ? NPU : 1][4];
+  const uint32_t vl = v0 + T * lane;
+  uint32_t xs[T], ov[T];
+  uint32_t pl[NPU > 0 ? NPU : 1][T];
 #pragma unroll
-  for (int b = 0; b < NPU; ++b)
+  for (int t = 0; t < T; ++t) {
+    xs[t] = ov[t] = 0;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) pl[b][t] = 0;
+    for (int b = 0; b < NPU; ++b) pl[b][t] = 0;
+  }
 #pragma unroll
-  for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < T; ++t) {
     const uint32_t v = vl + t;
     if (v < V) {
       const size_t a = (size_t)v * W + c;
@@ -927,7 +963,7 @@ __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint
     }
   }
 #pragma unroll
-  for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < T; ++t) {
     const uint32_t v = vl + t;
     if (v < V) {
       const size_t a = (size_t)v * W + c;
@@ -940,19 +976,22 @@ __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint
   const PassDesc* dsc = p.desc;
   if (dsc->reach) {
 #pragma unroll
-    for (int t = 0; t < 4; ++t)
+    for (int t = 0; t < T; ++t)
       if (vl + t < V) dsc->reach[(size_t)(vl + t) * dsc->reach_wpv + dsc->reach_col + c] = xs[t];
     return;
   }
   uint32_t* dist = dsc->dist;
   const uint32_t s0 = c * 32;
   const uint32_t jn = min(32u, P - s0);
-  const bool any_ovf = (ov[0] | ov[1] | ov[2] | ov[3]) != 0;
-  const bool full = vec_ok && vl + 3 < V;
-  for (uint32_t j = 0; j < jn; ++j) {
-    uint32_t dv[4];
+  uint32_t ovx = 0;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < T; ++t) ovx |= ov[t];
+  const bool any_ovf = ovx != 0;
+  const bool full = vec_ok && vl + T - 1 < V;
+  for (uint32_t j = 0; j < jn; ++j) {
+    uint32_t dv[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
       uint32_t val = 0;
 #pragma unroll
       for (int b = 0; b < NPU; ++b) val |= ((pl[b][t] >> j) & 1u) << b;
@@ -962,23 +1001,43 @@ __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint
     bool skip = false;
     if (any_ovf) {
 #pragma unroll
-      for (int t = 0; t < 4; ++t) skip |= ((ov[t] & xs[t]) >> j) & 1u;
+      for (int t = 0; t < T; ++t) skip |= ((ov[t] & xs[t]) >> j) & 1u;
     }
     if (full && !skip) {
-      *reinterpret_cast<uint4*>(row) = make_uint4(dv[0], dv[1], dv[2], dv[3]);
+      MatVec<T>::store(row, dv);
     } else {
 #pragma unroll
-      for (int t = 0; t < 4; ++t)
+      for (int t = 0; t < T; ++t)
         if (vl + t < V && !(((ov[t] & xs[t]) >> j) & 1u)) row[t] = dv[t];
     }
   }
 }
 
+// 32x32 bit-matrix transpose across a warp: lane j returns the word whose bit
+// t is bit j of lane t's x (five exchange steps of halving width).
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const uint32_t m = s == 16  ? 0x0000FFFFu
+                       : s == 8 ? 0x00FF00FFu
+                       : s == 4 ? 0x0F0F0F0Fu
+                       : s == 2 ? 0x33333333u
+                                : 0x55555555u;
+    const uint32_t y = __shfl_xor_sync(FULL, x, s);
+    x = (lane & s) ? ((x & ~m) | ((y & ~m) >> s)) : ((x & m) | ((y & m) << s));
+  }
+  return x;
+}
+
 // Per-source reductions straight from the visited words and level planes
 // (no S*V matrix): a warp item is word c of 1024 consecutive vertices, lane j
-// accumulates source 32c+j, and each lane loads one vertex's words which the
-// warp then walks with shuffles. The words read are zeroed like in the
-// materialisation; lanes flagged in ovf were accumulated by the level kernel.
+// accumulates source 32c+j, and each lane loads one vertex's words. Per 32
+// vertices the warp transposes the visited word and each level plane (32x32
+// bits), so lane j holds source j's bits over those vertices: the reached
+// count is a popcount, the distance sum a popcount per plane, the
+// eccentricity the largest plane pattern present. The words read are zeroed
+// like in the materialisation; lanes flagged in ovf were accumulated by the
+// level kernel.
 template <int W>
 __device__ void reduce_sources(const LevelParams& p, uint32_t P, uint32_t npu, bool use_ovf) {
   constexpr uint32_t CHUNK = 1024;
@@ -1015,21 +1074,27 @@ __device__ void reduce_sources(const LevelParams& p, uint32_t P, uint32_t npu, b
             p.planes[b * VW + a] = 0;
           }
       }
-      uint32_t live = __ballot_sync(FULL, x != 0);
-      while (live) {
-        const int t = __ffs(live) - 1;
-        live &= live - 1;
-        const uint32_t xt = __shfl_sync(FULL, x, t) & ~__shfl_sync(FULL, o, t);
-        uint32_t d = 0;
+      if (__ballot_sync(FULL, x != 0) == 0) continue;  // warp-uniform
+      const uint32_t xv = x & ~o;  // lanes with an in-plane distance
+      const uint32_t X = transpose32(xv, lane);
+      uint32_t Pt[MAT_NPMAX];
 #pragma unroll
-        for (int b = 0; b < MAT_NPMAX; ++b)
-          if (b < (int)npu) d |= ((__shfl_sync(FULL, pl[b], t) >> lane) & 1u) << b;
-        if ((xt >> lane) & 1u) {
-          sum += d;
-          ecc = max(ecc, d);
-          ++cnt;
+      for (int b = 0; b < MAT_NPMAX; ++b) {
+        Pt[b] = 0;
+        if (b < (int)npu) Pt[b] = transpose32(pl[b] & xv, lane);  // npu is warp-uniform
+      }
+      cnt += __popc(X);
+      uint32_t cand = X, e = 0;
+#pragma unroll
+      for (int b = MAT_NPMAX - 1; b >= 0; --b) {
+        sum += (unsigned long long)__popc(Pt[b]) << b;
+        const uint32_t hi = cand & Pt[b];
+        if (hi) {
+          cand = hi;
+          e |= 1u << b;
         }
       }
+      if (X) ecc = max(ecc, e);
     }
     if (cnt && 32 * c + lane < P) {
       SourceStats* s = st + 32 * c + lane;
@@ -1046,7 +1111,7 @@ __device__ void reduce_sources(const LevelParams& p, uint32_t P, uint32_t npu, b
 // starts from clean buffers. Warps take (vertex tile, word) items
 // independently: no shared memory, no barriers.
 template <int W>
-__global__ void __launch_bounds__(MAT_BLOCK, 4) materialize_kernel(LevelParams p) {
+__global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(LevelParams p) {
   const PassDesc* dsc = p.desc;
   const uint32_t P = dsc->num_sources;
   const uint32_t Wu = (P + 31) / 32;
