@@ -772,6 +772,9 @@ def run_ncu_case(args, spec):
     if args.ncu_case == "level":
         eng.run_ms_reachability(g, src)
         print("ncu case ok", json.dumps(eng.last_stats))
+    elif args.ncu_case == "reduce":
+        eng.run_ms_bfs_stats(g, src)
+        print("ncu case ok", json.dumps(eng.last_stats))
     else:
         import torch
         out = torch.empty(spec["S"] * g.num_vertices, dtype=torch.int32, device="cuda")
@@ -791,10 +794,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the served/batched summary of the default workload's line")
-    ap.add_argument("--ncu-case", choices=["level", "materialize"],
-                    help="one untimed run sized for an ncu capture: 'level' = the "
-                         "workload in reachability mode (no S*V matrix) with the level "
-                         "loop driven from the host so each level is a plain launch; "
+    ap.add_argument("--ncu-case", choices=["level", "materialize", "reduce"],
+                    help="one untimed run sized for an ncu capture, the level loop "
+                         "driven from the host so each level is a plain launch: "
+                         "'level' = the workload in reachability mode (no S*V matrix); "
+                         "'reduce' = the workload's per-source statistics; "
                          "'materialize' = R-MAT scale 21, S=512, one distance run")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]

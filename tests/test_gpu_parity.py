@@ -40,6 +40,9 @@ def _graphs(native):
         "tree": native.generate_random_tree(2000, 4),
         "wilson": native.wilson_grid(60, 50, 80, 5),
         "grid64": native.generate_grid2d(64, 64),
+        # odd V: per-plane arrays of V*W words start off 16-byte boundaries for W <= 2
+        "er_odd": native.generate_erdos_renyi_np(2999, 8 / 2998, 6),
+        "tree_odd": native.generate_random_tree(1001, 7),
     }
 
 

@@ -41,7 +41,10 @@ def test_source_stats_match_oracle(native, oracle, method):
         cases = [(native.generate_graph500_rmat(12, 16, 61), 700),
                  (native.wilson_grid(50, 40, 40, 7), 300),
                  (native.path_graph(1500), 5),  # levels beyond the 8 planes
-                 (native.generate_rmat(10, 8, 0.57, 0.19, 0.19, 0.05, 8, directed=True), 40)]
+                 (native.generate_rmat(10, 8, 0.57, 0.19, 0.19, 0.05, 8, directed=True), 40),
+                 # several vertex chunks, the last one ragged; 2- and 4-word passes
+                 (native.wilson_grid(71, 73, 40, 9), 33),
+                 (native.generate_graph500_rmat(13, 8, 62), 100)]
         for g, S in cases:
             src = np.random.default_rng(S).integers(0, g.num_vertices, S).astype(np.uint32)
             got = eng.run_ms_bfs_stats(g, src)

@@ -153,18 +153,25 @@ struct LevelKernelInfo {
   void* init;         // kernel symbols for graph nodes
   void* level;
   void* materialize;
+  void* reduce;       // per-source reductions in place of materialize
   void* cleanup;
   int level_block;
   int level_grid;
   int mat_block;
   int mat_grid;
   size_t mat_smem;
+  int red_block;
+  int red_grid;
 };
-// Fills kernel symbols and launch shapes for words-per-vertex W.
-bool level_kernel_info(uint32_t W, int num_sms, LevelKernelInfo* out);
+// Fills kernel symbols and launch shapes for words-per-vertex W and NP level
+// planes (the materialisation stages 1 + NP arrays in shared memory).
+bool level_kernel_info(uint32_t W, uint32_t NP, int num_sms, LevelKernelInfo* out);
+size_t materialize_smem_bytes(uint32_t W, uint32_t NP);
 void launch_init(const LevelParams& p, cudaStream_t s);
 void launch_level(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s);
-void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s);
+// reduce: per-source reductions (reduce_kernel) instead of rows or bitmasks.
+void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
+                        cudaStream_t s);
 void launch_cleanup(const LevelParams& p, cudaStream_t s);
 
 struct CtaParams {

@@ -73,11 +73,15 @@ struct Workspace {
   PassDesc* d_desc = nullptr;
   LevelRec* d_log = nullptr;
   std::vector<void*> allocs;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  // One instantiated pass per finishing kernel: [0] materialise, [1] reduce
+  // (built on first use).
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
   ~Workspace() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
+    for (int i = 0; i < 2; ++i) {
+      if (exec[i]) cudaGraphExecDestroy(exec[i]);
+      if (graph[i]) cudaGraphDestroy(graph[i]);
+    }
     for (void* a : allocs) cudaFree(a);
   }
 };
@@ -212,10 +216,12 @@ int dev_alloc(msbfs_engine* eng, Workspace* w, void** ptr, size_t bytes) {
   return MSBFS_OK;
 }
 
-int build_graph_exec(msbfs_engine* eng, Workspace* w) {
+// reduce: the pass ends in reduce_kernel (per-source reductions) instead of
+// materialize_kernel.
+int build_graph_exec(msbfs_engine* eng, Workspace* w, bool reduce) {
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
-  w->graph = g;
+  w->graph[reduce] = g;
   cudaGraphNode_t n_mctl, n_mst, n_init, n_cond, n_lvl, n_mat, n_clean;
   cudaMemsetParams m1{};
   m1.dst = w->d_ctl;
@@ -282,10 +288,10 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w) {
   CK(cudaGraphAddKernelNode(&n_lvl, body, nullptr, 0, &kl));
 
   cudaKernelNodeParams km{};
-  km.func = w->k.materialize;
-  km.gridDim = dim3(w->k.mat_grid);
-  km.blockDim = dim3(w->k.mat_block);
-  km.sharedMemBytes = (unsigned)w->k.mat_smem;
+  km.func = reduce ? w->k.reduce : w->k.materialize;
+  km.gridDim = dim3(reduce ? w->k.red_grid : w->k.mat_grid);
+  km.blockDim = dim3(reduce ? w->k.red_block : w->k.mat_block);
+  km.sharedMemBytes = reduce ? 0u : (unsigned)w->k.mat_smem;
   km.kernelParams = args_p;
   CK(cudaGraphAddKernelNode(&n_mat, g, &n_cond, 1, &km));
 
@@ -299,7 +305,7 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w) {
   (void)n_lvl;
   (void)n_mat;
   (void)n_clean;
-  CK(cudaGraphInstantiate(&w->exec, g, 0));
+  CK(cudaGraphInstantiate(&w->exec[reduce], g, 0));
   return MSBFS_OK;
 }
 
@@ -317,11 +323,14 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   w->graph_id = g->id;
   w->W = W;
   w->mode = mode;
-  if (!level_kernel_info(W, eng->num_sms, &w->k))
+  const uint32_t dist_bits = bit_length_u64(g->V > 1 ? g->V - 1 : 1);
+  const uint32_t NP = std::min<uint32_t>(dist_bits, 8);
+  if (!level_kernel_info(W, NP, eng->num_sms, &w->k))
     return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "unsupported words per vertex");
   // Work is claimed dynamically, so a smaller grid is only slower, never wrong.
   w->k.level_grid = std::max(1, (int)((uint64_t)w->k.level_grid * eng->sm_share / 100));
   w->k.mat_grid = std::max(1, (int)((uint64_t)w->k.mat_grid * eng->sm_share / 100));
+  w->k.red_grid = std::max(1, (int)((uint64_t)w->k.red_grid * eng->sm_share / 100));
   LevelParams& p = w->p;
   p.V = (uint32_t)g->V;
   p.W = W;
@@ -331,8 +340,7 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   p.in_off = g->coff;
   p.in_idx = g->cidx;
   const size_t VW = g->V * (size_t)W;
-  const uint32_t dist_bits = bit_length_u64(g->V > 1 ? g->V - 1 : 1);
-  p.NP = std::min<uint32_t>(dist_bits, 8);
+  p.NP = NP;
   p.qcap = (uint32_t)std::min<uint64_t>(g->V + g->E / eng->seg + 1, 0xFFFFFFFFull);
   p.mode = mode;
   p.alpha = eng->alpha;
@@ -384,7 +392,7 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)std::max(p.hlive_words, 1u) * 4))) return rc;
   p.hlive = (uint32_t*)ptr;
   if (!eng->host_loop) {
-    rc = build_graph_exec(eng, w.get());
+    rc = build_graph_exec(eng, w.get(), false);
     if (rc) {
       // Conditional graph nodes unavailable: fall back to the host-driven loop.
       eng->host_loop = true;
@@ -411,7 +419,7 @@ int ensure_events(msbfs_engine* eng, size_t n) {
 // Profiling form of the host-driven loop: one level kernel at a time with a
 // CUDA event on each side, then the materialisation likewise. The last entry
 // of the returned vector is the materialisation.
-int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
+int run_pass_profiled(msbfs_engine* eng, Workspace* w, bool reduce, std::vector<float>* ms) {
   int rc;
   CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
   CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
@@ -436,7 +444,7 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
     if (L > w->p.max_levels) return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
   }
   CK(cudaEventRecord(eng->lvl_events[0], eng->stream));
-  launch_materialize(w->p, w->k, eng->stream);
+  launch_materialize(w->p, w->k, reduce, eng->stream);
   CK(cudaEventRecord(eng->lvl_events[1], eng->stream));
   launch_cleanup(w->p, eng->stream);
   CK(cudaGetLastError());
@@ -447,7 +455,7 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, std::vector<float>* ms) {
   return MSBFS_OK;
 }
 
-int run_pass_host_loop(msbfs_engine* eng, Workspace* w) {
+int run_pass_host_loop(msbfs_engine* eng, Workspace* w, bool reduce) {
   CK(cudaMemsetAsync(w->d_ctl, 0, sizeof(LevelCtl), eng->stream));
   CK(cudaMemsetAsync(w->p.stamp, 0xFF, w->p.V * sizeof(uint32_t), eng->stream));
   CK(cudaMemsetAsync(w->p.fbits[0], 0, 3 * ((w->p.V + 31) / 32) * sizeof(uint32_t), eng->stream));
@@ -465,7 +473,7 @@ int run_pass_host_loop(msbfs_engine* eng, Workspace* w) {
     if (launched > (uint64_t)w->p.max_levels + 16)
       return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
   }
-  launch_materialize(w->p, w->k, eng->stream);
+  launch_materialize(w->p, w->k, reduce, eng->stream);
   launch_cleanup(w->p, eng->stream);
   CK(cudaGetLastError());
   return MSBFS_OK;
@@ -586,6 +594,12 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   const size_t passes = (S + PW - 1) / PW;
   Workspace* w = nullptr;
   if ((rc = get_workspace(eng, g, W, mode, &w))) return rc;
+  const bool reduce = stats_dev != nullptr;
+  if (reduce && !eng->host_loop && w->exec[0] && !w->exec[1] &&
+      build_graph_exec(eng, w, true) != MSBFS_OK) {
+    eng->host_loop = true;
+    cudaGetLastError();
+  }
   if (passes > eng->h_ctl_cap) {
     CK(cudaStreamSynchronize(eng->stream));
     if (eng->h_ctl) cudaFreeHost(eng->h_ctl);
@@ -624,11 +638,11 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     // stack descriptor can go out of scope.
     CK(cudaMemcpyAsync(w->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, eng->stream));
     if (eng->profiling >= 2) {
-      if ((rc = run_pass_profiled(eng, w, &eng->pass_event_ms[ps]))) return rc;
-    } else if (w->exec && !eng->host_loop) {
-      CK(cudaGraphLaunch(w->exec, eng->stream));
+      if ((rc = run_pass_profiled(eng, w, reduce, &eng->pass_event_ms[ps]))) return rc;
+    } else if (w->exec[reduce] && !eng->host_loop) {
+      CK(cudaGraphLaunch(w->exec[reduce], eng->stream));
     } else {
-      if ((rc = run_pass_host_loop(eng, w))) return rc;
+      if ((rc = run_pass_host_loop(eng, w, reduce))) return rc;
     }
     CK(cudaMemcpyAsync(&eng->h_ctl[ps], w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost,
                        eng->stream));

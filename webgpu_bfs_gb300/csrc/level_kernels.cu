@@ -897,101 +897,98 @@ __global__ void init_kernel(LevelParams p) {
 
 __device__ __forceinline__ uint32_t bit_length(uint32_t x) { return x ? 32 - __clz(x) : 0; }
 
-// Materialisation: a work item is word c (sources 32c .. 32c+31 of the
-// pass) of MAT_TV consecutive vertices, MAT_VPL per lane, so each distance
-// row is written with 8- or 16-byte stores. On R-MAT scale 22, S=512: 2
-// vertices per lane (8-byte stores, 40 registers, 6 blocks per SM) 3.9 ms;
-// 4 per lane (16-byte stores, 64 registers, 4 blocks) 5.4 ms; 1 per lane
-// (4-byte stores) 8.7 ms.
-#ifndef MSBFS_MAT_VPL
-#define MSBFS_MAT_VPL 2
-#endif
-constexpr int MAT_VPL = MSBFS_MAT_VPL;  // vertices per lane: 2 or 4
-constexpr int MAT_TV = 32 * MAT_VPL;    // vertices per work item
+// Materialisation. A block stages a tile of the visited words and level
+// planes in shared memory, one coalesced 16-byte load per thread per array
+// (MAT_TILE_WORDS words, 4 KB), transposed to [word][vertex] so that a warp
+// reads one word of 64 consecutive vertices without bank conflicts. Each of
+// the 16 (word, 64-vertex segment) columns of a tile then gives 32 distance
+// rows, written as 256-byte segments (one 8-byte store per lane per row).
+// Staging keeps every global load coalesced; the earlier form, where each
+// lane loaded one 4-byte word per vertex (64-byte stride) and relied on the
+// warps sharing a tile to meet in L1, ran 3.9 to 5.6 ms on R-MAT scale 22,
+// S=512 depending on how closely those warps kept in step.
+constexpr int MAT_TILE_WORDS = MAT_BLOCK * 4;
 constexpr int MAT_NPMAX = 8;
-constexpr int MAT_MIN_BLOCKS = MAT_VPL == 4 ? 4 : 6;
+constexpr int MAT_COLS = 16;  // (word, 64-vertex segment) columns per tile
+#ifndef MSBFS_MAT_MIN_BLOCKS
+#define MSBFS_MAT_MIN_BLOCKS 5
+#endif
+constexpr int MAT_MIN_BLOCKS = MSBFS_MAT_MIN_BLOCKS;
 
-template <int N>
-struct MatVec;
-template <>
-struct MatVec<4> {
-  static __device__ __forceinline__ void store(uint32_t* row, const uint32_t (&d)[4]) {
-    *reinterpret_cast<uint4*>(row) = make_uint4(d[0], d[1], d[2], d[3]);
-  }
-};
-template <>
-struct MatVec<2> {
-  static __device__ __forceinline__ void store(uint32_t* row, const uint32_t (&d)[2]) {
-    *reinterpret_cast<uint2*>(row) = make_uint2(d[0], d[1]);
-  }
+template <int W>
+struct MatGeo {
+  static constexpr int TW = W <= 16 ? W : 16;     // words per vertex in a tile
+  static constexpr int TV = MAT_TILE_WORDS / TW;  // vertices per tile
+  // Shared row stride in words: even (8-byte column reads) and, for TW = 16,
+  // conflict-free for the transposing stores (bank = 8q + 2k + vertex).
+  static constexpr int RS = TV + 2;
+  static constexpr int ARR = TW * RS;             // shared words per array
+  static_assert(TW * (TV / 64) == MAT_COLS, "16 columns per tile");
 };
 
-// One work item: word c of the MAT_TV vertices from v0, i.e. the 32 sources
-// 32c .. 32c+31 of this pass. Lane l owns vertices v0 + MAT_VPL*l onwards: it
-// loads their visited / overflow / plane words (strided by W words; the warps
-// of a block take consecutive words of the same vertices, so the 32-byte
-// sectors are shared through L1), zeroes them, and writes the 32 distance
-// rows as contiguous segments (one MAT_VPL-word store per lane per row). NPU
-// (planes in use) is a template argument so the plane words stay in
-// registers.
-template <int NPU>
-__device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint32_t c,
-                                         uint32_t lane, uint32_t P, bool use_ovf,
-                                         bool vec_ok) {
-  constexpr int T = MAT_VPL;
-  const uint32_t W = p.W;
+// Output side of a pass, read from the descriptor once per thread.
+struct MatOut {
+  uint32_t* dist;
+  uint32_t* reach;
+  uint32_t reach_wpv, reach_col;
+};
+
+// Writes the rows of column cs of the staged tile: word cw = g*TW + c of the
+// 64 vertices from v0 + 64*seg, i.e. sources 32cw .. 32cw+31 of the pass.
+// Lane l owns vertices 2l and 2l+1 of the segment. NPU (planes in use) is a
+// template argument so the plane words stay in registers. Lanes flagged in
+// ovf (deeper than the planes encode) were written by the level kernel and
+// are skipped.
+template <int W, int NPU>
+__device__ __forceinline__ void mat_column(const LevelParams& p, const MatOut& out,
+                                           const uint32_t* sh, uint32_t v0, uint32_t g,
+                                           uint32_t cs, uint32_t lane, uint32_t P, bool use_ovf,
+                                           bool vec_ok) {
+  using G = MatGeo<W>;
   const uint32_t V = p.V;
-  const size_t VW = (size_t)V * W;
-  const uint32_t vl = v0 + T * lane;
-  uint32_t xs[T], ov[T];
-  uint32_t pl[NPU > 0 ? NPU : 1][T];
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    xs[t] = ov[t] = 0;
-#pragma unroll
-    for (int b = 0; b < NPU; ++b) pl[b][t] = 0;
+  const uint32_t c = cs % G::TW;
+  const uint32_t seg = cs / G::TW;
+  const uint32_t cw = g * G::TW + c;
+  const uint32_t vloc = seg * 64 + 2 * lane;
+  const uint32_t vl = v0 + vloc;
+  uint32_t xs[2], ov[2] = {0, 0};
+  uint32_t pl[NPU > 0 ? NPU : 1][2];
+  {
+    const uint2 t = *reinterpret_cast<const uint2*>(sh + c * G::RS + vloc);
+    xs[0] = t.x;
+    xs[1] = t.y;
   }
 #pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const uint32_t v = vl + t;
-    if (v < V) {
-      const size_t a = (size_t)v * W + c;
-      xs[t] = p.vis[a];
-      if (use_ovf) ov[t] = p.ovf[a];
+  for (int b = 0; b < NPU; ++b) {
+    const uint2 t = *reinterpret_cast<const uint2*>(sh + (1 + b) * G::ARR + c * G::RS + vloc);
+    pl[b][0] = t.x;
+    pl[b][1] = t.y;
+  }
+  if (use_ovf) {
 #pragma unroll
-      for (int b = 0; b < NPU; ++b) pl[b][t] = p.planes[b * VW + a];
+    for (int t = 0; t < 2; ++t) {
+      if (vl + t < V) {
+        uint32_t* a = p.ovf + (size_t)(vl + t) * W + cw;
+        ov[t] = *a;
+        if (ov[t]) *a = 0;
+      }
     }
   }
+  if (out.reach) {
 #pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const uint32_t v = vl + t;
-    if (v < V) {
-      const size_t a = (size_t)v * W + c;
-      p.vis[a] = 0;
-      if (use_ovf) p.ovf[a] = 0;
-#pragma unroll
-      for (int b = 0; b < NPU; ++b) p.planes[b * VW + a] = 0;
-    }
-  }
-  const PassDesc* dsc = p.desc;
-  if (dsc->reach) {
-#pragma unroll
-    for (int t = 0; t < T; ++t)
-      if (vl + t < V) dsc->reach[(size_t)(vl + t) * dsc->reach_wpv + dsc->reach_col + c] = xs[t];
+    for (int t = 0; t < 2; ++t)
+      if (vl + t < V) out.reach[(size_t)(vl + t) * out.reach_wpv + out.reach_col + cw] = xs[t];
     return;
   }
-  uint32_t* dist = dsc->dist;
-  const uint32_t s0 = c * 32;
+  uint32_t* dist = out.dist;
+  const uint32_t s0 = cw * 32;
   const uint32_t jn = min(32u, P - s0);
-  uint32_t ovx = 0;
-#pragma unroll
-  for (int t = 0; t < T; ++t) ovx |= ov[t];
-  const bool any_ovf = ovx != 0;
-  const bool full = vec_ok && vl + T - 1 < V;
+  const bool any_ovf = (ov[0] | ov[1]) != 0;
+  const bool full = vec_ok && vl + 1 < V;
   for (uint32_t j = 0; j < jn; ++j) {
-    uint32_t dv[T];
+    uint32_t dv[2];
 #pragma unroll
-    for (int t = 0; t < T; ++t) {
+    for (int t = 0; t < 2; ++t) {
       uint32_t val = 0;
 #pragma unroll
       for (int b = 0; b < NPU; ++b) val |= ((pl[b][t] >> j) & 1u) << b;
@@ -999,15 +996,12 @@ __device__ __forceinline__ void mat_item(const LevelParams& p, uint32_t v0, uint
     }
     uint32_t* row = dist + (size_t)(s0 + j) * V + vl;
     bool skip = false;
-    if (any_ovf) {
-#pragma unroll
-      for (int t = 0; t < T; ++t) skip |= ((ov[t] & xs[t]) >> j) & 1u;
-    }
+    if (any_ovf) skip = (((ov[0] & xs[0]) | (ov[1] & xs[1])) >> j) & 1u;
     if (full && !skip) {
-      MatVec<T>::store(row, dv);
+      *reinterpret_cast<uint2*>(row) = make_uint2(dv[0], dv[1]);
     } else {
 #pragma unroll
-      for (int t = 0; t < T; ++t)
+      for (int t = 0; t < 2; ++t)
         if (vl + t < V && !(((ov[t] & xs[t]) >> j) & 1u)) row[t] = dv[t];
     }
   }
@@ -1029,117 +1023,203 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
   return x;
 }
 
-// Per-source reductions straight from the visited words and level planes
-// (no S*V matrix): a warp item is word c of 1024 consecutive vertices, lane j
-// accumulates source 32c+j, and each lane loads one vertex's words. Per 32
-// vertices the warp transposes the visited word and each level plane (32x32
-// bits), so lane j holds source j's bits over those vertices: the reached
-// count is a popcount, the distance sum a popcount per plane, the
-// eccentricity the largest plane pattern present. The words read are zeroed
-// like in the materialisation; lanes flagged in ovf were accumulated by the
-// level kernel.
+constexpr int RED_BLOCK = 256;
+constexpr int RED_MIN_BLOCKS = 2;
+constexpr uint32_t RED_CHUNK = 2048;  // vertices per reduction work item
+
+template <int VEC>
+__device__ __forceinline__ bool any_word(const Words<VEC>& x) {
+  uint32_t a = 0;
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) a |= x.w[j];
+  return a != 0;
+}
+
+// Per-source reductions (distance sum, reached count, eccentricity) straight
+// from the visited words and level planes, with no S*V matrix. A warp item is
+// one group of G = min(4, W) words of RED_CHUNK consecutive vertices; lane l
+// loads the group of vertex vb + l as one vector (the next tile's visited
+// group is fetched while this one is reduced). For each word c of the group
+// the warp transposes the visited word and each level plane (32x32 bits), so
+// lane j holds source 32c+j's bits over the 32 vertices: the reached count is
+// a popcount, the distance sum a popcount per plane, the eccentricity the
+// largest plane pattern present. Plane bits are a subset of visited bits, so
+// tiles without a visited bit skip the plane loads, and only words read
+// non-zero are written back as zero (the next pass starts from clean
+// buffers). Lanes flagged in ovf (deeper than the planes encode) were folded
+// in by the level kernel.
 template <int W>
-__device__ void reduce_sources(const LevelParams& p, uint32_t P, uint32_t npu, bool use_ovf) {
-  constexpr uint32_t CHUNK = 1024;
+__global__ void __launch_bounds__(RED_BLOCK, RED_MIN_BLOCKS) reduce_kernel(LevelParams p) {
+  constexpr int G = W >= 4 ? 4 : W;
+  const PassDesc* dsc = p.desc;
+  SourceStats* st = dsc->stats;
+  if (!st) return;
+  const uint32_t P = dsc->num_sources;
   const uint32_t Wu = (P + 31) / 32;
+  const uint32_t ngroups = (Wu + G - 1) / G;
+  const uint32_t dmax = p.ctl->level;
+  const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
+  const bool use_ovf = dmax >= (1u << p.NP);
   const uint32_t lane = threadIdx.x & 31;
   const size_t VW = (size_t)p.V * W;
-  SourceStats* st = p.desc->stats;
-  const size_t nitems = (size_t)((p.V + CHUNK - 1) / CHUNK) * Wu;
+  const size_t nitems = (size_t)((p.V + RED_CHUNK - 1) / RED_CHUNK) * ngroups;
   const size_t warp_g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
   const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  Words<G> zero;
+#pragma unroll
+  for (int j = 0; j < G; ++j) zero.w[j] = 0;
   for (size_t it = warp_g; it < nitems; it += nwarps) {
-    const uint32_t c = (uint32_t)(it % Wu);
-    const uint32_t v0 = (uint32_t)(it / Wu) * CHUNK;
-    const uint32_t v_end = min(v0 + CHUNK, p.V);
-    unsigned long long sum = 0;
-    uint32_t ecc = 0, cnt = 0;
+    const uint32_t g = (uint32_t)(it % ngroups);
+    const uint32_t v0 = (uint32_t)(it / ngroups) * RED_CHUNK;
+    const uint32_t v_end = min(v0 + RED_CHUNK, p.V);
+    unsigned long long sum[G];
+    uint32_t cnt[G], ecc[G];
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      sum[i] = 0;
+      cnt[i] = ecc[i] = 0;
+    }
+    Words<G> xn = zero;
+    if (v0 + lane < v_end) xn = ld_words<G>(p.vis + (size_t)(v0 + lane) * W + (size_t)g * G);
     for (uint32_t vb = v0; vb < v_end; vb += 32) {
       const uint32_t v = vb + lane;
-      uint32_t x = 0, o = 0, pl[MAT_NPMAX];
+      const size_t a = (size_t)v * W + (size_t)g * G;
+      const Words<G> x = xn;
+      xn = zero;
+      if (v + 32 < v_end) xn = ld_words<G>(p.vis + a + 32 * (size_t)W);
+      const bool any = any_word(x);
+      if (__ballot_sync(FULL, any) == 0) continue;  // warp-uniform
+      Words<G> o = zero, pl[MAT_NPMAX];
 #pragma unroll
-      for (int b = 0; b < MAT_NPMAX; ++b) pl[b] = 0;
-      if (v < v_end) {
-        const size_t a = (size_t)v * W + c;
-        x = p.vis[a];
-        p.vis[a] = 0;
-        if (use_ovf) {
-          o = p.ovf[a];
-          p.ovf[a] = 0;
-        }
+      for (int b = 0; b < MAT_NPMAX; ++b) pl[b] = zero;
+      if (any) {
+        st_words<G>(p.vis + a, zero);
+        if (use_ovf) o = ld_words<G>(p.ovf + a);
 #pragma unroll
         for (int b = 0; b < MAT_NPMAX; ++b)
-          if (b < (int)npu) {
-            pl[b] = p.planes[b * VW + a];
-            p.planes[b * VW + a] = 0;
+          if (b < (int)npu) pl[b] = ld_words<G>(p.planes + b * VW + a);
+        if (any_word(o)) st_words<G>(p.ovf + a, zero);
+#pragma unroll
+        for (int b = 0; b < MAT_NPMAX; ++b)
+          if (b < (int)npu && any_word(pl[b])) st_words<G>(p.planes + b * VW + a, zero);
+      }
+#pragma unroll
+      for (int i = 0; i < G; ++i) {
+        if (__ballot_sync(FULL, x.w[i] != 0) == 0) continue;  // warp-uniform
+        const uint32_t xv = x.w[i] & ~o.w[i];  // lanes with an in-plane distance
+        const uint32_t X = transpose32(xv, lane);
+        cnt[i] += __popc(X);
+        uint32_t cand = X, e = 0;
+#pragma unroll
+        for (int b = MAT_NPMAX - 1; b >= 0; --b) {
+          if (b >= (int)npu) continue;  // npu is warp-uniform
+          const uint32_t Pt = transpose32(pl[b].w[i] & xv, lane);
+          sum[i] += (unsigned long long)__popc(Pt) << b;
+          const uint32_t hi = cand & Pt;
+          if (hi) {
+            cand = hi;
+            e |= 1u << b;
           }
-      }
-      if (__ballot_sync(FULL, x != 0) == 0) continue;  // warp-uniform
-      const uint32_t xv = x & ~o;  // lanes with an in-plane distance
-      const uint32_t X = transpose32(xv, lane);
-      uint32_t Pt[MAT_NPMAX];
-#pragma unroll
-      for (int b = 0; b < MAT_NPMAX; ++b) {
-        Pt[b] = 0;
-        if (b < (int)npu) Pt[b] = transpose32(pl[b] & xv, lane);  // npu is warp-uniform
-      }
-      cnt += __popc(X);
-      uint32_t cand = X, e = 0;
-#pragma unroll
-      for (int b = MAT_NPMAX - 1; b >= 0; --b) {
-        sum += (unsigned long long)__popc(Pt[b]) << b;
-        const uint32_t hi = cand & Pt[b];
-        if (hi) {
-          cand = hi;
-          e |= 1u << b;
         }
+        if (X) ecc[i] = max(ecc[i], e);
       }
-      if (X) ecc = max(ecc, e);
     }
-    if (cnt && 32 * c + lane < P) {
-      SourceStats* s = st + 32 * c + lane;
-      atomicAdd(&s->sum, sum);
-      atomicMax(&s->ecc, ecc);
-      atomicAdd(&s->reached, cnt);
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      const uint32_t s = 32 * (g * G + i) + lane;
+      if (cnt[i] && s < P) {
+        atomicAdd(&st[s].sum, sum[i]);
+        atomicMax(&st[s].ecc, ecc[i]);
+        atomicAdd(&st[s].reached, cnt[i]);
+      }
     }
   }
 }
 
 // Turns visited words + level planes into the source-major u32 distance rows
-// (or copies the visited words out as a reachability bitmask, or reduces them
-// to per-source statistics) and zeroes the words it read, so the next pass
-// starts from clean buffers. Warps take (vertex tile, word) items
-// independently: no shared memory, no barriers.
+// (or copies the visited words out as a reachability bitmask) and zeroes the
+// words it read, so the next pass starts from clean buffers. Blocks take
+// (vertex tile, word group) items; see MatGeo for the tile. Passes that want
+// per-source reductions run reduce_kernel instead.
 template <int W>
 __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(LevelParams p) {
+  using G = MatGeo<W>;
+  extern __shared__ uint32_t mat_sh[];  // [1 + NP][TW][RS]: visited words, then planes
   const PassDesc* dsc = p.desc;
+  if (dsc->stats) return;
   const uint32_t P = dsc->num_sources;
   const uint32_t Wu = (P + 31) / 32;
   const uint32_t dmax = p.ctl->level;
   const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
   const bool use_ovf = dmax >= (1u << p.NP);
-  if (dsc->stats) {
-    reduce_sources<W>(p, P, npu, use_ovf);
-    return;
-  }
-  const uint32_t lane = threadIdx.x & 31;
-  const bool vec_ok = (p.V % 4 == 0) && (((uintptr_t)dsc->dist & 15) == 0);
-  const size_t ntiles = (p.V + MAT_TV - 1) / MAT_TV;
-  const size_t nitems = ntiles * Wu;
-  const size_t warp_g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
-  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-  for (size_t it = warp_g; it < nitems; it += nwarps) {
-    const uint32_t v0 = (uint32_t)(it / Wu) * MAT_TV;
-    const uint32_t c = (uint32_t)(it % Wu);
-    switch (npu) {
-#define MAT_CASE(n) \
-  case n: mat_item<n>(p, v0, c, lane, P, use_ovf, vec_ok); break;
-      MAT_CASE(0) MAT_CASE(1) MAT_CASE(2) MAT_CASE(3) MAT_CASE(4)
-      MAT_CASE(5) MAT_CASE(6) MAT_CASE(7) MAT_CASE(8)
-#undef MAT_CASE
-      default: break;
+  const MatOut out{dsc->dist, dsc->reach, dsc->reach_wpv, dsc->reach_col};
+  const uint32_t V = p.V;
+  const size_t VW = (size_t)V * W;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t lane = tid & 31;
+  const uint32_t warp = tid >> 5;
+  const bool vec_ok = (V % 2 == 0) && (((uintptr_t)out.dist & 7) == 0);
+  const uint32_t ngu = (Wu + G::TW - 1) / G::TW;  // word groups in use
+  const size_t nitems = (size_t)((V + G::TV - 1) / G::TV) * ngu;
+  const uint32_t o = 4 * tid;  // tile word offset of this thread's four words
+  // Plane b starts b*V*W words into the planes buffer: 16-byte aligned only
+  // when V*W is a multiple of 4 (always for W >= 4).
+  const bool vec_planes = VW % 4 == 0;
+  for (size_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const uint32_t g = (uint32_t)(it % ngu);
+    const uint32_t v0 = (uint32_t)(it / ngu) * G::TV;
+    // Global word index of this thread's four words: the tile is contiguous
+    // when a vertex's words fit in one group (W <= 16); otherwise it is 64
+    // runs of 16 words.
+    size_t gw;
+    bool inb;
+    if constexpr (W <= 16) {
+      gw = (size_t)v0 * W + o;
+      inb = gw + 3 < VW;
+    } else {
+      gw = (size_t)(v0 + o / 16) * W + 16 * g + (o % 16);
+      inb = v0 + o / 16 < V;
     }
+    for (uint32_t a = 0; a <= npu; ++a) {
+      uint32_t* src = a == 0 ? p.vis : p.planes + (size_t)(a - 1) * VW;
+      uint32_t x[4] = {0, 0, 0, 0};
+      if (inb && (a == 0 || vec_planes)) {
+        const uint4 t = *reinterpret_cast<const uint4*>(src + gw);
+        x[0] = t.x; x[1] = t.y; x[2] = t.z; x[3] = t.w;
+        if (t.x | t.y | t.z | t.w) *reinterpret_cast<uint4*>(src + gw) = make_uint4(0, 0, 0, 0);
+      } else if constexpr (W <= 16) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (gw + k < VW) {
+            x[k] = src[gw + k];
+            if (x[k]) src[gw + k] = 0;
+          }
+      }
+      uint32_t* dst = mat_sh + a * G::ARR;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) dst[((o + k) % G::TW) * G::RS + (o + k) / G::TW] = x[k];
+    }
+    __syncthreads();
+    for (uint32_t cs = warp; cs < MAT_COLS; cs += MAT_BLOCK / 32) {
+      if (g * G::TW + cs % G::TW >= Wu) continue;  // no sources in this word
+      switch (npu) {
+#define MAT_CASE(n) \
+  case n: mat_column<W, n>(p, out, mat_sh, v0, g, cs, lane, P, use_ovf, vec_ok); break;
+        MAT_CASE(0) MAT_CASE(1) MAT_CASE(2) MAT_CASE(3) MAT_CASE(4)
+        MAT_CASE(5) MAT_CASE(6) MAT_CASE(7) MAT_CASE(8)
+#undef MAT_CASE
+        default: break;
+      }
+    }
+    __syncthreads();
   }
+}
+
+size_t materialize_smem_bytes(uint32_t W, uint32_t NP) {
+  const uint32_t tw = W <= 16 ? W : 16;
+  const uint32_t tv = MAT_TILE_WORDS / tw;
+  const uint32_t np = NP < (uint32_t)MAT_NPMAX ? NP : (uint32_t)MAT_NPMAX;
+  return (size_t)(1 + np) * tw * (tv + 2) * sizeof(uint32_t);
 }
 
 // Zeroes the last frontier (level L_end) after the loop has stopped.
@@ -1179,10 +1259,11 @@ __global__ void traversed_edges_kernel(uint32_t V, const uint32_t* __restrict__ 
 // ------------------------------------------------------------------ host side
 
 template <int W>
-static void fill_info(int num_sms, LevelKernelInfo* k) {
+static void fill_info(int num_sms, uint32_t NP, LevelKernelInfo* k) {
   k->init = (void*)init_kernel<W>;
   k->level = (void*)level_kernel<W>;
   k->materialize = (void*)materialize_kernel<W>;
+  k->reduce = (void*)reduce_kernel<W>;
   k->cleanup = (void*)cleanup_kernel<W>;
   k->level_block = LEVEL_BLOCK;
   int occ = 0;
@@ -1190,22 +1271,28 @@ static void fill_info(int num_sms, LevelKernelInfo* k) {
   if (occ < 1) occ = 1;
   k->level_grid = num_sms * occ;
   k->mat_block = MAT_BLOCK;
-  k->mat_smem = 0;
+  k->mat_smem = materialize_smem_bytes(W, NP);
   int mocc = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mocc, materialize_kernel<W>, MAT_BLOCK, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mocc, materialize_kernel<W>, MAT_BLOCK,
+                                                k->mat_smem);
   if (mocc < 1) mocc = 1;
   k->mat_grid = num_sms * mocc;
+  k->red_block = RED_BLOCK;
+  int rocc = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, reduce_kernel<W>, RED_BLOCK, 0);
+  if (rocc < 1) rocc = 1;
+  k->red_grid = num_sms * rocc;
 }
 
-bool level_kernel_info(uint32_t W, int num_sms, LevelKernelInfo* out) {
+bool level_kernel_info(uint32_t W, uint32_t NP, int num_sms, LevelKernelInfo* out) {
   switch (W) {
-    case 1: fill_info<1>(num_sms, out); return true;
-    case 2: fill_info<2>(num_sms, out); return true;
-    case 4: fill_info<4>(num_sms, out); return true;
-    case 8: fill_info<8>(num_sms, out); return true;
-    case 16: fill_info<16>(num_sms, out); return true;
-    case 32: fill_info<32>(num_sms, out); return true;
-    case 64: fill_info<64>(num_sms, out); return true;
+    case 1: fill_info<1>(num_sms, NP, out); return true;
+    case 2: fill_info<2>(num_sms, NP, out); return true;
+    case 4: fill_info<4>(num_sms, NP, out); return true;
+    case 8: fill_info<8>(num_sms, NP, out); return true;
+    case 16: fill_info<16>(num_sms, NP, out); return true;
+    case 32: fill_info<32>(num_sms, NP, out); return true;
+    case 64: fill_info<64>(num_sms, NP, out); return true;
     default: return false;
   }
 }
@@ -1243,18 +1330,23 @@ void launch_level(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s
 }
 
 template <int W>
-static void launch_mat_t(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
-  materialize_kernel<W><<<k.mat_grid, k.mat_block, k.mat_smem, s>>>(p);
+static void launch_mat_t(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
+                         cudaStream_t s) {
+  if (reduce)
+    reduce_kernel<W><<<k.red_grid, k.red_block, 0, s>>>(p);
+  else
+    materialize_kernel<W><<<k.mat_grid, k.mat_block, k.mat_smem, s>>>(p);
 }
-void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
+void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
+                        cudaStream_t s) {
   switch (p.W) {
-    case 1: launch_mat_t<1>(p, k, s); break;
-    case 2: launch_mat_t<2>(p, k, s); break;
-    case 4: launch_mat_t<4>(p, k, s); break;
-    case 8: launch_mat_t<8>(p, k, s); break;
-    case 16: launch_mat_t<16>(p, k, s); break;
-    case 32: launch_mat_t<32>(p, k, s); break;
-    case 64: launch_mat_t<64>(p, k, s); break;
+    case 1: launch_mat_t<1>(p, k, reduce, s); break;
+    case 2: launch_mat_t<2>(p, k, reduce, s); break;
+    case 4: launch_mat_t<4>(p, k, reduce, s); break;
+    case 8: launch_mat_t<8>(p, k, reduce, s); break;
+    case 16: launch_mat_t<16>(p, k, reduce, s); break;
+    case 32: launch_mat_t<32>(p, k, reduce, s); break;
+    case 64: launch_mat_t<64>(p, k, reduce, s); break;
   }
 }
 
