@@ -19,6 +19,18 @@ def test_request_stream_shapes(native):
     assert all(np.array_equal(a, b) for a, b in zip(reqs, again))  # seeded
 
 
+def test_small_request_workload_spec(native):
+    spec = bench.WORKLOADS["served_rmat22_small"]
+    assert max(spec["sizes"]) <= 64 and spec["server"]["express_slots"] == 0
+    # the same R-MAT scale 22 graph as the default workload, so the default
+    # line can reuse it
+    assert spec["graph"] == {k: bench.WORKLOADS["rmat22_s512"][k]
+                             for k in ("kind", "scale", "ef", "seed")}
+    g = native.wilson_grid(40, 40, 30, 3)
+    reqs = bench.make_requests(g, 120, spec["seed"], spec["sizes"])
+    assert {int(r.size) for r in reqs} == set(spec["sizes"])
+
+
 def test_poisson_arrivals_rate():
     assert np.all(bench.poisson_arrivals(5, None, 0) == 0)
     t = bench.poisson_arrivals(20000, 50.0, 3)
