@@ -151,8 +151,7 @@ class ClockSampler:
 
 
 def level_bytes(rec, V, W, E):
-    """Algorithmic bytes of one level-kernel launch (per-unit figures stated in
-    the design doc): bottom-up reads the in-offsets once, the visited row of every
+    """Algorithmic bytes of one level-kernel launch: bottom-up reads the in-offsets once, the visited row of every
     vertex with lanes left to discover, an index per in-neighbour examined
     and a W-word frontier row per in-neighbour in the frontier, and writes visited + frontier rows of newly reached vertices and
     4 bytes per discovered distance; top-down reads its queue entries, the

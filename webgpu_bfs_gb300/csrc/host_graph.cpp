@@ -1,7 +1,7 @@
 // Host graph core: CSR/CSC construction, validation and seeded generators.
 // Restates crates/core/src/graph.rs and crates/core/src/generators.rs of the
 // reference in C++17; the big builders (R-MAT symmetrisation, transpose) run
-// on all host cores because BASELINE-sized graphs (R-MAT scale 22-24, up to
+// on all host cores because the benchmark graphs (R-MAT scale 22-24, up to
 // half a billion directed edges) are built before every benchmark.
 #include "host_graph.h"
 
