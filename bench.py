@@ -802,6 +802,21 @@ def run_ncu_case(args, spec):
     import webgpu_bfs_gb300 as m
     if args.ncu_case == "materialize":
         spec = dict(kind="rmat", scale=21, ef=16, S=512, seed=20221)
+    if args.ncu_case == "batched":
+        # the tuned configuration: the first run writes the autotuner's cache,
+        # later runs read it, so their only batch_kernel launch is b.run()
+        # A quarter of the 1,000-graph batch (same distributions) keeps the
+        # device footprint of the capture near 3 GB.
+        import tempfile
+        spec = dict(WORKLOADS["batched1000"], n_er=150, n_grid=75, n_rmat=25)
+        b = m.BatchedBfs(make_batch(m, spec))
+        b.autotune(samples_per_class=3,
+                   cache_path=os.path.join(tempfile.gettempdir(), "msbfs_batch250_tune.txt"))
+        print("ncu case ok", b.run())
+        b.close()
+        return
+    if args.ncu_case == "cta":
+        spec = WORKLOADS["road_s2048"]
     g = make_graph(m, spec)
     src = m.sample_sources(g, spec["S"], spec["seed"], min_degree=1)
     eng = m.GpuBfsEngine(m.GpuBfsMethod.Auto)
@@ -811,6 +826,11 @@ def run_ncu_case(args, spec):
     elif args.ncu_case == "reduce":
         eng.run_ms_bfs_stats(g, src)
         print("ncu case ok", json.dumps(eng.last_stats))
+    elif args.ncu_case == "cta":
+        import torch
+        out = torch.empty(spec["S"] * g.num_vertices, dtype=torch.int32, device="cuda")
+        eng.run_ms_bfs_device(g, src, out.data_ptr())
+        print("ncu case ok", json.dumps(eng.synchronize()))
     else:
         import torch
         out = torch.empty(spec["S"] * g.num_vertices, dtype=torch.int32, device="cuda")
@@ -830,12 +850,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the served/batched summary of the default workload's line")
-    ap.add_argument("--ncu-case", choices=["level", "materialize", "reduce"],
+    ap.add_argument("--ncu-case", choices=["level", "materialize", "reduce", "cta", "batched"],
                     help="one untimed run sized for an ncu capture, the level loop "
                          "driven from the host so each level is a plain launch: "
                          "'level' = the workload in reachability mode (no S*V matrix); "
                          "'reduce' = the workload's per-source statistics; "
-                         "'materialize' = R-MAT scale 21, S=512, one distance run")
+                         "'materialize' = R-MAT scale 21, S=512, one distance run; "
+                         "'cta' = road 339x338, S=2048 (CTA-per-source path); "
+                         "'batched' = 250 graphs of the batched configuration, tuned")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
     if args.ncu_case:

@@ -11,7 +11,8 @@
 //   ovf[V][W]        lanes whose distance did not fit NP planes; those were
 //                    written straight into the distance matrix
 //   Q[3][qcap]       u64 queue entries (seg << 32 | v): frontier vertices, one
-//                    entry per SEG out-edges so hub expansion is split
+//                    entry per SEG out-edges so hub expansion is split (Q[0]
+//                    holds V + E/SEG0 entries: the sources' queue uses SEG0)
 //   stamp[V]         level at which v was last enqueued by a top-down step
 #pragma once
 
@@ -131,6 +132,7 @@ struct LevelParams {
   uint32_t alpha;     // push -> pull when m_f * alpha > unexplored edges
   uint32_t beta;      // pull -> push when n_f * beta < V
   uint32_t seg;       // out-edges per queue entry
+  uint32_t seg0;      // out-edges per entry of the sources' queue (level 0)
   uint32_t heavy;     // in-degree from which a whole warp scans one vertex
   uint32_t max_levels;
   uint32_t split;     // in-degree above which in-edges are sliced across warps

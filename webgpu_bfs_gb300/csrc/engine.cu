@@ -32,6 +32,13 @@
 
 using namespace msbfs;
 
+#ifndef MSBFS_PUSH_SEG
+#define MSBFS_PUSH_SEG 64
+#endif
+#ifndef MSBFS_PUSH_SEG0
+#define MSBFS_PUSH_SEG0 8  // out-edges per entry of the sources' queue
+#endif
+
 namespace {
 
 struct Workspace;
@@ -129,7 +136,7 @@ struct msbfs_engine {
   uint32_t max_words = 16;
   uint32_t alpha = 14;
   uint32_t beta = 24;
-  uint32_t seg = 64;
+  uint32_t seg = MSBFS_PUSH_SEG;  // out-edges per top-down queue entry
 #ifndef MSBFS_HEAVY
 #define MSBFS_HEAVY 32
 #endif
@@ -341,11 +348,15 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   p.in_idx = g->cidx;
   const size_t VW = g->V * (size_t)W;
   p.NP = NP;
+  // A level's queue holds each vertex once (the stamp), so V + E/seg
+  // entries bound it; the sources' queue (slot 0 at level 0) uses seg0.
   p.qcap = (uint32_t)std::min<uint64_t>(g->V + g->E / eng->seg + 1, 0xFFFFFFFFull);
+  const uint64_t qcap0 = std::min<uint64_t>(g->V + g->E / MSBFS_PUSH_SEG0 + 1, 0xFFFFFFFFull);
   p.mode = mode;
   p.alpha = eng->alpha;
   p.beta = eng->beta;
   p.seg = eng->seg;
+  p.seg0 = std::min<uint32_t>(MSBFS_PUSH_SEG0, eng->seg);
   p.heavy = eng->heavy;
   p.bits_div = eng->bits_div;
   p.max_levels = (uint32_t)std::min<uint64_t>(g->V + 2, 0xFFFFFFF0ull);
@@ -367,7 +378,7 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   if ((rc = dev_alloc(eng, w.get(), &ptr, VW * 4))) return rc;
   p.ovf = (uint32_t*)ptr;
   for (int i = 0; i < 3; ++i) {
-    if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)p.qcap * 8))) return rc;
+    if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)(i == 0 ? qcap0 : p.qcap) * 8))) return rc;
     p.Q[i] = (unsigned long long*)ptr;
   }
   if ((rc = dev_alloc(eng, w.get(), &ptr, g->V * 4))) return rc;

@@ -135,9 +135,9 @@ struct BlockQueue {
 
 // Enqueue straight into the global queue (sources, and blocks whose staging
 // area is full). Entry i of vertex v covers out-edges [i*seg, (i+1)*seg).
-__device__ void enqueue_global(const LevelParams& p, uint32_t slot, uint32_t v) {
+__device__ void enqueue_global(const LevelParams& p, uint32_t slot, uint32_t v, uint32_t seg) {
   const uint32_t deg = p.out_off[v + 1] - p.out_off[v];
-  const uint32_t n = nseg_of(deg, p.seg);
+  const uint32_t n = nseg_of(deg, seg);
   const uint32_t base = atomicAdd(&p.ctl->qcount[slot], n);
   atomicAdd(&p.ctl->qverts[slot], 1u);
   atomicAdd(&p.ctl->qedges[slot], (unsigned long long)deg);
@@ -151,7 +151,7 @@ __device__ __forceinline__ void bq_push(const LevelParams& p, BlockQueue& bq, ui
   if (pos < BQ_CAP)
     bq.items[pos] = v;
   else
-    enqueue_global(p, slot, v);
+    enqueue_global(p, slot, v, p.seg);
 }
 
 // Compacts the block's staged vertices into the global queue with one
@@ -661,6 +661,9 @@ __device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
   const uint32_t k0 = lig * VEC;
   const uint32_t d = L + 1;
   const uint32_t si = L % 3, so = (L + 1) % 3;
+  // The sources' queue (level 0) uses shorter entries: a few hundred
+  // sources would otherwise leave most groups idle behind long edge walks.
+  const uint32_t seg = L == 0 ? p.seg0 : p.seg;
   const uint32_t* __restrict__ Fin = p.F[si];
   uint32_t* __restrict__ Fout = p.F[so];
   const unsigned long long* __restrict__ Qi = p.Q[si];
@@ -674,13 +677,23 @@ __device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     const uint32_t sg = (uint32_t)(ent >> 32);
     const Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
     const uint32_t ob = __ldg(p.out_off + u), oe = __ldg(p.out_off + u + 1);
-    const uint32_t eb = ob + sg * p.seg;
-    const uint32_t ee = min(oe, eb + p.seg);
+    const uint32_t eb = ob + sg * seg;
+    const uint32_t ee = min(oe, eb + seg);
     if (lig == 0) cnt.edges += ee - eb;
+    // The next edge's target and its visited words are fetched while this
+    // edge is processed. A stale visited word only widens `needed`; the
+    // atomicOr's previous value decides what is new.
+    uint32_t vn = eb < ee ? __ldg(p.out_idx + eb) : 0u;
+    Words<VEC> vwn;
+    if (eb < ee) vwn = ldcg_words<VEC>(p.vis + (size_t)vn * W + k0);
     for (uint32_t e = eb; e < ee; ++e) {
-      const uint32_t v = __ldg(p.out_idx + e);
+      const uint32_t v = vn;
       uint32_t* vrow = p.vis + (size_t)v * W + k0;
-      const Words<VEC> vw = ldcg_words<VEC>(vrow);
+      const Words<VEC> vw = vwn;
+      if (e + 1 < ee) {
+        vn = __ldg(p.out_idx + e + 1);
+        vwn = ldcg_words<VEC>(p.vis + (size_t)vn * W + k0);
+      }
       bool found = false;
 #pragma unroll
       for (int q = 0; q < VEC; ++q) {
@@ -885,7 +898,7 @@ __global__ void init_kernel(LevelParams p) {
     atomicOr(p.F[0] + w, bit);
     atomicOr(&p.ctl->lanes[0][i >> 5], bit);
     atomicOr(p.fbits[0] + (s >> 5), 1u << (s & 31));
-    if (atomicExch(p.stamp + s, 0u) != 0u) enqueue_global(p, 0, s);
+    if (atomicExch(p.stamp + s, 0u) != 0u) enqueue_global(p, 0, s, p.seg0);
     ++ok;
   }
   if (ok) atomicAdd(&p.ctl->pairs, ok);
