@@ -91,7 +91,8 @@ typedef struct msbfs_stats {
   uint32_t levels;           /* max BFS levels over passes                   */
   uint32_t push_levels;      /* summed over passes                           */
   uint32_t pull_levels;      /* summed over passes                           */
-  uint32_t reserved0;
+  uint32_t cta_cluster;      /* CTA path: blocks per cluster sharing a source's
+                                visited bitmap (0: one block per source)     */
   uint64_t reached_pairs;    /* (s, v) pairs with a finite distance          */
   double gpu_ms;             /* device time of the whole call (CUDA events)  */
 } msbfs_stats;

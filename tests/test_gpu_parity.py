@@ -217,25 +217,53 @@ def test_page_locked_host_output(native, oracle):
         eng.close()
 
 
-def test_cta_global_bitmap_beyond_shared_memory(native, oracle):
+@pytest.mark.parametrize("mode", ["global", "cluster"])
+def test_cta_global_bitmap_beyond_shared_memory(native, oracle, monkeypatch, mode):
     """Road graph whose visited bitmap exceeds shared memory (1,960,000
-    vertices > 8 bits x 227 KB): the CTA path keeps its bitmap in an
-    L2-resident global slab per block. Rows, statistics and the queue slab
-    that alternates ends by level are checked over thousands of levels."""
+    vertices > 8 bits x 227 KB). Calls of few sources split the bitmap over
+    the shared memory of a thread-block cluster (rank 0 traverses, the other
+    ranks' slices are reached through distributed shared memory); otherwise
+    (here forced by MSBFS_CTA_CLUSTER=0) each block keeps an L2-resident
+    global slab. Rows, statistics and the queue slab that alternates ends by
+    level are checked over thousands of levels."""
+    monkeypatch.setenv("MSBFS_CTA_CLUSTER", "0" if mode == "global" else "-1")
     g = native.wilson_grid(1400, 1400, 2000, 11)
     src = native.sample_sources(g, 20, 4)
     eng = native.GpuBfsEngine(native.GpuBfsMethod.WorkgroupPersistentBfs)
     try:
         got = eng.run_ms_bfs(g, src)
         assert eng.last_stats["path"] == 4  # CTA path, not the level-path fallback
+        if mode == "global":
+            assert eng.last_stats["cta_cluster"] == 0
+        else:
+            assert eng.last_stats["cta_cluster"] in (2, 4, 8)
         want = _oracle(oracle, g, src)
-        assert_same(got, want, g, src, "global-bitmap CTA rows")
+        assert_same(got, want, g, src, f"{mode}-bitmap CTA rows")
         st = eng.run_ms_bfs_stats(g, src)
         d = want.reshape(len(src), g.num_vertices).astype(np.int64)
         fin = d != 0xFFFFFFFF
         assert np.array_equal(st["reached"], fin.sum(1))
         assert np.array_equal(st["eccentricity"], np.where(fin, d, 0).max(1))
         assert np.array_equal(st["distance_sum"], np.where(fin, d, 0).sum(1))
+    finally:
+        eng.close()
+
+
+def test_cta_cluster_sizes(native, oracle, monkeypatch):
+    """Clusters of 2, 4 and 8 blocks: a 9,000,000-vertex grid needs 8 slices
+    (1.1 MB of bitmap), a 4,000,000-vertex one 4 (forced even with more
+    sources than resident clusters), each with sources in odd slices."""
+    monkeypatch.setenv("MSBFS_CTA_CLUSTER", "1")
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.WorkgroupPersistentBfs)
+    try:
+        for side, want_cl in ((3000, 8), (2000, 4), (1500, 2)):
+            g = native.generate_grid2d(side, side)
+            V = g.num_vertices
+            src = np.asarray([V - 1, V // 2 + side // 2, 5 * V // 8, 1], np.uint32)
+            got = eng.run_ms_bfs(g, src)
+            assert eng.last_stats["path"] == 4
+            assert eng.last_stats["cta_cluster"] == want_cl
+            assert_same(got, _oracle(oracle, g, src), g, src, f"cluster grid {side}")
     finally:
         eng.close()
 

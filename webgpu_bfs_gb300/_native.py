@@ -27,13 +27,13 @@ class Stats(C.Structure):
         ("levels", C.c_uint32),
         ("push_levels", C.c_uint32),
         ("pull_levels", C.c_uint32),
-        ("reserved0", C.c_uint32),
+        ("cta_cluster", C.c_uint32),
         ("reached_pairs", C.c_uint64),
         ("gpu_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved0"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class LevelRecord(C.Structure):

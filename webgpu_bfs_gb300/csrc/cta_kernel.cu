@@ -7,17 +7,23 @@
 // bitmap in shared memory and synchronises only inside the block, so a
 // ~1,000-level traversal needs no grid-wide step. The GB300 form differs:
 // the bitmap takes up to ~227 KB of shared memory (vs 14 KB) and, for larger
-// graphs, moves to an L2-resident global slab per block instead of giving up
-// the path; the frontier queues live in one L2-resident global slab of V
+// graphs, is split over the shared memory of a thread-block cluster (calls of
+// few sources) or moves to an L2-resident global slab per block instead of
+// giving up the path; the frontier queues live in one L2-resident global slab of V
 // words per resident block (no overflow fallback), distances are exact u32
 // written into the caller's row, and the grid is persistent: each resident
 // block pulls the next source from an atomic cursor until all sources are
 // done. No block ever waits on another.
+#include <cooperative_groups.h>
+
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 
 #include "../../include/msbfs.h"
 #include "device_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace msbfs {
 
@@ -37,6 +43,18 @@ constexpr size_t CTA_GLOBAL_SCRATCH_BYTES = 4ull << 30;
 // Frontier entries per shared-memory queue half (16 KB of vertex ids, 32 KB
 // of edge ranges).
 constexpr uint32_t CTA_SMEM_QUEUE = 4096;
+// Cluster form: threads of rank 0 (which walks every frontier) and edge
+// records each keeps in flight. Road 1448 x 1448, one source: 1,024 threads
+// and 4 records 9.8 ms, 1,024 and 2 10.6 ms, 512 and 4 12.3 ms (global-bitmap
+// mode 17.6 ms).
+#ifndef MSBFS_CTA_CLUSTER_THREADS
+#define MSBFS_CTA_CLUSTER_THREADS 1024
+#endif
+constexpr int CTA_CLUSTER_THREADS = MSBFS_CTA_CLUSTER_THREADS;
+#ifndef MSBFS_CTA_CLUSTER_ER_BATCH
+#define MSBFS_CTA_CLUSTER_ER_BATCH 4
+#endif
+constexpr int CTA_CLUSTER_ER_BATCH = MSBFS_CTA_CLUSTER_ER_BATCH;
 
 // GB: the visited bitmap lives in an L2-resident global slab per block (for
 // graphs whose bitmap does not fit shared memory) instead of shared memory.
@@ -201,6 +219,158 @@ __global__ void __launch_bounds__(CTA_THREADS, MINB) cta_bfs_kernel(CtaParams p)
   }
 }
 
+// Cluster form, for graphs whose visited bitmap does not fit one block's
+// shared memory. A cluster of CL blocks serves one source at a time: block
+// rank r keeps bitmap words [r*wpb, (r+1)*wpb) in its shared memory, and
+// rank 0 runs the traversal exactly as cta_bfs_kernel does, setting visited
+// bits of the other ranks' words with atomicOr through distributed shared
+// memory (one hop inside the GPC instead of an L2 round trip). The other
+// ranks zero their slice before a traversal and fill the unreached vertices
+// of their slice after it. Two cluster barriers per source: (1) the source
+// index is in every block and every slice is zero, (2) the traversal is done.
+// The queue (shared-memory halves in rank 0, then one global slab of V words
+// per cluster) and the edge records work as in cta_bfs_kernel.
+template <int CL, bool ER>
+__global__ void __launch_bounds__(CTA_CLUSTER_THREADS, 1) cta_cluster_kernel(CtaParams p) {
+  constexpr int CTA_ER_BATCH = CTA_CLUSTER_ER_BATCH;
+  extern __shared__ __align__(16) uint32_t smem_dyn[];
+  __shared__ uint32_t s_src_idx;  // written into every block by rank 0
+  __shared__ uint32_t s_cnt[3];
+  __shared__ unsigned long long s_sum;
+  __shared__ uint32_t s_reached;
+  cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t rank = cluster.block_rank();
+  const uint32_t V = p.V;
+  const uint32_t words = (V + 31) / 32;
+  const uint32_t wpb = (words + CL - 1) / CL;  // bitmap words per block
+  const uint32_t w0 = min(words, rank * wpb);
+  const uint32_t w1 = min(words, w0 + wpb);
+  uint32_t* bits = smem_dyn;  // this block's slice: words [w0, w1)
+  const uint32_t QH = p.qh;
+  uint32_t* sq = smem_dyn + (wpb + 1) / 2 * 2;
+  uint2* sq2 = reinterpret_cast<uint2*>(sq);
+  uint32_t* slab = p.gqueue + (size_t)(blockIdx.x / CL) * V;
+  auto slab_at = [&](uint32_t lv, uint32_t i) -> uint32_t* {
+    return (lv & 1) ? slab + (V - 1 - i) : slab + i;
+  };
+  auto q_get = [&](uint32_t lv, uint32_t i, uint32_t* eb, uint32_t* ee) {
+    if constexpr (ER) {
+      if (i < QH) {
+        const uint2 r = sq2[(lv & 1) * QH + i];
+        *eb = r.x;
+        *ee = r.y;
+        return;
+      }
+    }
+    const uint32_t u = i < QH ? sq[(lv & 1) * QH + i] : *slab_at(lv, i);
+    *eb = __ldg(p.off + u);
+    *ee = __ldg(p.off + u + 1);
+  };
+  auto q_put = [&](uint32_t lv, uint32_t i, uint32_t v, uint32_t eb, uint32_t ee) {
+    if (i < QH) {
+      if constexpr (ER)
+        sq2[(lv & 1) * QH + i] = make_uint2(eb, ee);
+      else
+        sq[(lv & 1) * QH + i] = v;
+    } else {
+      *slab_at(lv, i) = v;
+    }
+  };
+  // Word w of the whole bitmap: in this block's slice (rank 0's own) or in
+  // the owning block's, reached through distributed shared memory.
+  auto word_ptr = [&](uint32_t w, bool* local) -> uint32_t* {
+    const uint32_t o = w / wpb;
+    uint32_t* at = bits + (w - o * wpb);
+    *local = o == rank;
+    return *local ? at : cluster.map_shared_rank(at, o);
+  };
+
+  for (;;) {
+    if (rank == 0 && threadIdx.x == 0) {
+      const uint32_t si = atomicAdd(p.work, 1u);
+      for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(&s_src_idx, r) = si;
+      s_sum = 0;
+      s_reached = 0;
+      s_cnt[0] = s_cnt[1] = s_cnt[2] = 0;
+    }
+    for (uint32_t i = threadIdx.x; i < w1 - w0; i += blockDim.x) bits[i] = 0;
+    cluster.sync();  // (1)
+    const uint32_t si = s_src_idx;
+    if (si >= p.num_sources) break;  // the same value in every block
+    const uint32_t src = p.sources[si];
+    uint32_t* row = p.dist ? p.dist + (size_t)si * V : nullptr;
+    uint32_t ecc = 0;
+    if (rank == 0) {
+      if (threadIdx.x == 0) {
+        bool loc;
+        atomicOr(word_ptr(src >> 5, &loc), 1u << (src & 31));
+        if (row) row[src] = 0;
+        q_put(0, 0, src, __ldg(p.off + src), __ldg(p.off + src + 1));
+      }
+      uint32_t n_in = 1;
+      uint32_t level = 0;
+      unsigned long long my_sum = 0;
+      uint32_t my_cnt = 0;
+      __syncthreads();
+      while (n_in) {
+        ecc = level;
+        const uint32_t nd = level + 1;
+        uint32_t* cnt = &s_cnt[level % 3];
+        if (threadIdx.x == 0) s_cnt[(level + 1) % 3] = 0;
+        for (uint32_t i = threadIdx.x; i < n_in; i += blockDim.x) {
+          uint32_t eb, ee;
+          q_get(level, i, &eb, &ee);
+          for (uint32_t e = eb; e < ee; e += (ER ? CTA_ER_BATCH : 1)) {
+            uint4 r[ER ? CTA_ER_BATCH : 1];
+            if constexpr (ER) {
+#pragma unroll
+              for (int k = 0; k < CTA_ER_BATCH; ++k)
+                if (e + k < ee) r[k] = __ldg(p.erec + e + k);
+            } else {
+              r[0] = make_uint4(__ldg(p.idx + e), 0u, 0u, 0u);
+            }
+#pragma unroll
+            for (int k = 0; k < (ER ? CTA_ER_BATCH : 1); ++k) {
+              if (e + k >= ee) break;
+              const uint32_t v = r[k].x;
+              const uint32_t bit = 1u << (v & 31);
+              bool loc;
+              uint32_t* wp = word_ptr(v >> 5, &loc);
+              if (loc && (*wp & bit)) continue;  // a remote pre-check costs the atomic's hop
+              const uint32_t old = atomicOr(wp, bit);
+              if (old & bit) continue;
+              if (row) row[v] = nd;
+              my_sum += nd;
+              ++my_cnt;
+              q_put(level + 1, atomicAdd(cnt, 1u), v, r[k].y, r[k].z);
+            }
+          }
+        }
+        __syncthreads();
+        n_in = *cnt;
+        ++level;
+      }
+      if (p.stats && my_cnt) {
+        atomicAdd(&s_sum, my_sum);
+        atomicAdd(&s_reached, my_cnt);
+      }
+    }
+    cluster.sync();  // (2)
+    if (row) {
+      // Unreached vertices of this block's slice.
+      const uint32_t vb = w0 * 32, ve = min(V, w1 * 32);
+      for (uint32_t v = vb + threadIdx.x; v < ve; v += blockDim.x)
+        if (!((bits[(v >> 5) - w0] >> (v & 31)) & 1u)) row[v] = CTA_DIST_MAX;
+    }
+    if (rank == 0 && p.stats && threadIdx.x == 0) {
+      p.stats[si].sum = s_sum;
+      p.stats[si].reached = s_reached + 1;
+      p.stats[si].ecc = ecc;
+    }
+    __syncthreads();  // the slice is read above and zeroed at the top
+  }
+}
+
 // Edge records of a road-like graph: for every edge e = (u, v), {v, off[v],
 // off[v+1], 0}. One thread per vertex u.
 __global__ void edge_records_kernel(uint32_t V, const uint32_t* __restrict__ off,
@@ -241,6 +411,88 @@ static int cta_occupancy(int minb, int block, size_t smem) {
                                      : cta_occupancy<GB, ER, CTA_MINB_LATENCY>(block, smem);
 }
 
+template <int CL, bool ER>
+static void* cta_cluster_fn() {
+  return (void*)cta_cluster_kernel<CL, ER>;
+}
+
+static void* cluster_kernel(int cl, bool er) {
+  switch (cl) {
+    case 2: return er ? cta_cluster_fn<2, true>() : cta_cluster_fn<2, false>();
+    case 4: return er ? cta_cluster_fn<4, true>() : cta_cluster_fn<4, false>();
+    case 8: return er ? cta_cluster_fn<8, true>() : cta_cluster_fn<8, false>();
+    default: return nullptr;
+  }
+}
+
+// Clusters that can be resident at once for a cluster launch of `cl` blocks
+// with `smem` bytes of dynamic shared memory each (0 if it cannot launch).
+static int cluster_capacity(int cl, bool er, size_t smem, int block) {
+  void* fn = cluster_kernel(cl, er);
+  if (!fn) return 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(cl);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr{};
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = cl;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+// Cluster mode for a call of few sources: the smallest cluster whose slices
+// hold the bitmap next to rank 0's queue halves. MSBFS_CTA_CLUSTER=0 turns
+// it off, =1 uses it whatever the number of sources.
+static bool cta_cluster_shape(uint32_t V, int sms, int optin, bool edge_records,
+                              size_t num_sources, CtaShape* out) {
+  const char* env = getenv("MSBFS_CTA_CLUSTER");
+  const int mode = env ? atoi(env) : -1;
+  if (mode == 0) return false;
+  const size_t words = ((size_t)V + 31) / 32;
+  const size_t entry = edge_records ? 2 * sizeof(uint32_t) : sizeof(uint32_t);
+  const size_t slack = 2048;
+  for (int cl : {2, 4, 8}) {
+    const size_t wpb = (words + cl - 1) / cl;
+    const size_t slice = (wpb + 1) / 2 * 2 * sizeof(uint32_t);
+    if (slice + 2 * 1024 * entry + slack > (size_t)optin) continue;
+    const size_t room = (size_t)optin - slack - slice;
+    CtaShape sh{};
+    sh.block = CTA_CLUSTER_THREADS;
+    sh.edge_records = edge_records;
+    sh.cluster = cl;
+    sh.minb = 1;
+    sh.qh = (uint32_t)std::min<size_t>(CTA_SMEM_QUEUE, room / (2 * entry) / 32 * 32);
+    sh.smem = slice + 2 * (size_t)sh.qh * entry;
+    const int n = cluster_capacity(cl, edge_records, sh.smem, sh.block);
+    if (n < 1) continue;
+    // A cluster traverses a source faster than a global-bitmap block, but a
+    // global-bitmap launch keeps several blocks per SM busy: clusters pay
+    // off while every source has a cluster of its own (road 1448 x 1448:
+    // S=64 10.7 vs 18.8 ms; S=152, two sources per cluster, 21.2 vs 22.1;
+    // S=256 46.3 vs 28.0 with a 512-thread rank 0).
+    if (mode != 1 && num_sources > (size_t)n) return false;
+    sh.grid = n * cl;
+    (void)sms;
+    *out = sh;
+    return true;
+  }
+  return false;
+}
+
 bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
                       size_t num_sources, CtaShape* out) {
   int sms = 0, optin = 0, per_sm = 0;
@@ -251,6 +503,8 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_recor
   const size_t entry = edge_records ? 2 * sizeof(uint32_t) : sizeof(uint32_t);
   const bool shared_bits = (size_t)V <= cta_max_vertices(device);
   if (!shared_bits && !allow_global) return false;
+  if (!shared_bits && cta_cluster_shape(V, sms, optin, edge_records, num_sources, out))
+    return true;
   CtaShape sh{};
   sh.block = CTA_THREADS;
   sh.edge_records = edge_records;
@@ -298,6 +552,24 @@ void launch_cta(const CtaParams& params, const CtaShape& sh, int grid, cudaStrea
   CtaParams p = params;
   p.qh = sh.qh;  // the dynamic shared memory holds exactly these queue halves
   if (!sh.edge_records) p.erec = nullptr;
+  if (sh.cluster > 1) {
+    // grid: blocks, a multiple of the cluster size (checked by the caller)
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(sh.block);
+    cfg.dynamicSmemBytes = sh.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = sh.cluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    void* args[] = {&p};
+    cudaLaunchKernelExC(&cfg, cluster_kernel(sh.cluster, sh.edge_records), args);
+    return;
+  }
   if (sh.global_bits) {
     if (sh.edge_records)
       launch_cta_t<true, true>(p, sh, grid, s);

@@ -198,10 +198,14 @@ struct CtaShape {
   int minb = 3;           // register budget: resident blocks per SM it is built for
   bool global_bits = false;
   bool edge_records = false;
+  int cluster = 0;        // > 1: blocks per cluster sharing one source's bitmap
 };
 // Max V for the shared-memory visited bitmap; launch shape of the CTA kernel
-// for a call of num_sources sources (global-bitmap mode above that V when
-// allow_global; edge-range queue entries when the graph has edge records).
+// for a call of num_sources sources (above that V when allow_global: the
+// bitmap split over the shared memory of a thread-block cluster for calls of
+// few sources, an L2-resident global slab per block otherwise; edge-range
+// queue entries when the graph has edge records). In cluster mode `grid`
+// counts blocks (a multiple of `cluster`) and each cluster has one queue slab.
 size_t cta_max_vertices(int device);
 bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
                       size_t num_sources, CtaShape* out);

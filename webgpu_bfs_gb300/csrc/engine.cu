@@ -566,8 +566,11 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   const size_t V = g->V;
 
   if (path == MSBFS_PATH_CTA) {
-    const int blocks = std::min<int>(cta_grid, (int)S);
-    if ((rc = grow(eng, &eng->d_cta_queue, &eng->d_cta_queue_cap, (size_t)blocks * V)))
+    // Cluster mode: `blocks` stays a multiple of the cluster size, one
+    // queue slab per cluster.
+    const int cl = std::max(1, cta.cluster);
+    const int blocks = std::max(cl, std::min<int>(cta_grid, (int)std::min<size_t>(S * cl, 1u << 30)) / cl * cl);
+    if ((rc = grow(eng, &eng->d_cta_queue, &eng->d_cta_queue_cap, (size_t)(blocks / cl) * V)))
       return rc;
     if (cta.global_bits &&
         (rc = grow(eng, &eng->d_cta_bits, &eng->d_cta_bits_cap, (size_t)blocks * ((V + 31) / 32))))
@@ -588,6 +591,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     launch_cta(cp, cta, blocks, eng->stream);
     CK(cudaGetLastError());
     eng->last.passes = 1;
+    eng->last.cta_cluster = cta.cluster > 1 ? (uint32_t)cta.cluster : 0u;
     eng->last_passes = 0;
     if (host_out) {
       CK(cudaMemcpyAsync(host_out, dist_dev, S * V * sizeof(uint32_t), cudaMemcpyDeviceToHost,
