@@ -817,6 +817,8 @@ def run_ncu_case(args, spec):
         return
     if args.ncu_case == "cta":
         spec = WORKLOADS["road_s2048"]
+    if args.ncu_case == "cluster":
+        spec = dict(WORKLOADS["served_road1448"]["graph"], S=1)
     g = make_graph(m, spec)
     src = m.sample_sources(g, spec["S"], spec["seed"], min_degree=1)
     eng = m.GpuBfsEngine(m.GpuBfsMethod.Auto)
@@ -826,7 +828,7 @@ def run_ncu_case(args, spec):
     elif args.ncu_case == "reduce":
         eng.run_ms_bfs_stats(g, src)
         print("ncu case ok", json.dumps(eng.last_stats))
-    elif args.ncu_case == "cta":
+    elif args.ncu_case in ("cta", "cluster"):
         import torch
         out = torch.empty(spec["S"] * g.num_vertices, dtype=torch.int32, device="cuda")
         eng.run_ms_bfs_device(g, src, out.data_ptr())
@@ -850,13 +852,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the served/batched summary of the default workload's line")
-    ap.add_argument("--ncu-case", choices=["level", "materialize", "reduce", "cta", "batched"],
+    ap.add_argument("--ncu-case", choices=["level", "materialize", "reduce", "cta", "cluster",
+                                           "batched"],
                     help="one untimed run sized for an ncu capture, the level loop "
                          "driven from the host so each level is a plain launch: "
                          "'level' = the workload in reachability mode (no S*V matrix); "
                          "'reduce' = the workload's per-source statistics; "
                          "'materialize' = R-MAT scale 21, S=512, one distance run; "
                          "'cta' = road 339x338, S=2048 (CTA-per-source path); "
+                         "'cluster' = road 1448x1448, one source (cluster mode); "
                          "'batched' = 250 graphs of the batched configuration, tuned")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
