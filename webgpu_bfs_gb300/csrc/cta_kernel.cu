@@ -457,8 +457,8 @@ static int cluster_capacity(int cl, bool er, size_t smem, int block) {
 // Cluster mode for a call of few sources: the smallest cluster whose slices
 // hold the bitmap next to rank 0's queue halves. MSBFS_CTA_CLUSTER=0 turns
 // it off, =1 uses it whatever the number of sources.
-static bool cta_cluster_shape(uint32_t V, int optin, bool edge_records, size_t num_sources,
-                              uint32_t cluster_room, CtaShape* out) {
+static bool cta_cluster_shape(uint32_t V, int sms, int optin, bool edge_records,
+                              size_t num_sources, CtaShape* out) {
   const char* env = getenv("MSBFS_CTA_CLUSTER");
   const int mode = env ? atoi(env) : -1;
   if (mode == 0) return false;
@@ -484,8 +484,9 @@ static bool cta_cluster_shape(uint32_t V, int optin, bool edge_records, size_t n
     // off while every source has a cluster of its own (road 1448 x 1448:
     // S=64 10.7 vs 18.8 ms; S=152, two sources per cluster, 21.2 vs 22.1;
     // S=256 46.3 vs 28.0 with a 512-thread rank 0).
-    if (mode != 1 && num_sources * 100 > (size_t)n * cluster_room) return false;
+    if (mode != 1 && num_sources > (size_t)n) return false;
     sh.grid = n * cl;
+    (void)sms;
     *out = sh;
     return true;
   }
@@ -493,7 +494,7 @@ static bool cta_cluster_shape(uint32_t V, int optin, bool edge_records, size_t n
 }
 
 bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
-                      size_t num_sources, CtaShape* out, uint32_t cluster_room) {
+                      size_t num_sources, CtaShape* out) {
   int sms = 0, optin = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
@@ -502,8 +503,7 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_recor
   const size_t entry = edge_records ? 2 * sizeof(uint32_t) : sizeof(uint32_t);
   const bool shared_bits = (size_t)V <= cta_max_vertices(device);
   if (!shared_bits && !allow_global) return false;
-  if (!shared_bits &&
-      cta_cluster_shape(V, optin, edge_records, num_sources, cluster_room, out))
+  if (!shared_bits && cta_cluster_shape(V, sms, optin, edge_records, num_sources, out))
     return true;
   CtaShape sh{};
   sh.block = CTA_THREADS;

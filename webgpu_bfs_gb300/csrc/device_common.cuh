@@ -208,7 +208,7 @@ struct CtaShape {
 // counts blocks (a multiple of `cluster`) and each cluster has one queue slab.
 size_t cta_max_vertices(int device);
 bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_records,
-                      size_t num_sources, CtaShape* out, uint32_t cluster_room = 100);
+                      size_t num_sources, CtaShape* out);
 void launch_cta(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s);
 void launch_edge_records(uint32_t V, const uint32_t* off, const uint32_t* idx, uint4* erec,
                          cudaStream_t s);

@@ -147,10 +147,6 @@ struct msbfs_engine {
   uint32_t split = MSBFS_SPLIT;  // in-edge slice length of bottom-up steps
   uint32_t bits_div = 64;
   uint32_t sm_share = 100;  // percent of the resident grid the persistent kernels use
-  // Percent of the resident thread-block clusters the CTA path may count on
-  // being free (a served form's express slots share the GPU with the other
-  // slots' kernels): cluster mode only while every source gets one of them.
-  uint32_t cluster_room = 100;
   bool host_loop = false;
   bool zero_copy = true;  // MSBFS_ZERO_COPY=0 stages host output in HBM instead
   int profiling = 0;
@@ -553,8 +549,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   if (reach_dev && path == MSBFS_PATH_CTA) path = MSBFS_PATH_HYBRID;
   CtaShape cta{};
   if (path == MSBFS_PATH_CTA &&
-      !cta_launch_shape((uint32_t)g->V, eng->device, true, g->erec != nullptr, S, &cta,
-                        eng->cluster_room))
+      !cta_launch_shape((uint32_t)g->V, eng->device, true, g->erec != nullptr, S, &cta))
     path = MSBFS_PATH_HYBRID;
   const int cta_grid = std::max(1, (int)((uint64_t)cta.grid * eng->sm_share / 100));
   if (!g->sym && path != MSBFS_PATH_CTA && !g->coff)
@@ -1054,15 +1049,6 @@ int msbfs_graph_attach(msbfs_graph* g, msbfs_engine* e) {
     return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "graph lives on another device");
   if (e != g->eng && std::find(g->users.begin(), g->users.end(), e) == g->users.end())
     g->users.push_back(e);
-  return MSBFS_OK;
-}
-
-// Share of the resident clusters the CTA path of `e` may count on (see
-// msbfs_engine::cluster_room). Not part of the C ABI: set by the served form.
-int msbfs_engine_set_cluster_room(msbfs_engine* e, uint32_t percent) {
-  if (!e || percent < 1 || percent > 100) return MSBFS_ERR_INVALID_ARGUMENT;
-  std::lock_guard<std::mutex> lk(e->mu);
-  e->cluster_room = percent;
   return MSBFS_OK;
 }
 

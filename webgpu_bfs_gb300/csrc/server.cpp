@@ -18,10 +18,8 @@
 
 #include "../../include/msbfs.h"
 
-// engine.cu: lets a second engine of the device run on a resident graph;
-// sets the share of resident clusters an engine's CTA path may count on.
+// engine.cu: lets a second engine of the device run on a resident graph.
 int msbfs_graph_attach(msbfs_graph* g, msbfs_engine* e);
-int msbfs_engine_set_cluster_room(msbfs_engine* e, uint32_t percent);
 
 namespace {
 
@@ -319,13 +317,6 @@ int msbfs_server_create(int device, size_t V, size_t E, const uint32_t* ro, cons
     if ((rc = msbfs_engine_set_stream(sl.eng, sl.stream))) break;
     if (!sl.express && s->cfg.general_sm_percent < 100 &&
         (rc = msbfs_engine_set_sm_share(sl.eng, s->cfg.general_sm_percent)))
-      break;
-    // Express kernels find the SMs the general slots leave free: their CTA
-    // path uses thread-block clusters only for requests that fit there.
-    if (sl.express && s->cfg.express_slots < s->cfg.slots &&
-        (rc = msbfs_engine_set_cluster_room(
-             sl.eng, std::max<uint32_t>(1, 100 - std::min<uint32_t>(
-                                                  99, s->cfg.general_sm_percent)))))
       break;
     // One resident copy of the graph, shared by every slot's engine.
     if (k == 0 && (rc = msbfs_graph_create(sl.eng, V, E, ro, ci, &s->graph))) break;
