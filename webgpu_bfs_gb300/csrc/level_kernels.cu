@@ -34,9 +34,11 @@ constexpr int BQ_CAP = 2048;  // discovered vertices staged per block
 #define MSBFS_PULL_CH 4
 #endif
 #ifndef MSBFS_LEVEL_MIN_BLOCKS
-// 6 resident blocks of 256 threads (48 warps per SM): the bottom-up gathers
-// are latency-bound, and the extra warps outweigh the few spilled registers.
-#define MSBFS_LEVEL_MIN_BLOCKS 6
+// 8 resident blocks of 256 threads (all 64 warps of an SM, 32 registers):
+// the bottom-up gathers are latency-bound, and the extra warps outweigh the
+// spilled registers (R-MAT scale 22, S=512: dense levels 2.29 -> 1.92 ms
+// against 6 blocks at 40 registers; 4 and 5 blocks were slower still).
+#define MSBFS_LEVEL_MIN_BLOCKS 8
 #endif
 constexpr int CH = MSBFS_PULL_CH;  // in-neighbours gathered per chunk
 constexpr int MAT_BLOCK = 256;
