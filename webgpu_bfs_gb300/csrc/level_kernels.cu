@@ -1039,7 +1039,12 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
 }
 
 constexpr int RED_BLOCK = 256;
-constexpr int RED_MIN_BLOCKS = 2;
+#ifndef MSBFS_RED_MIN_BLOCKS
+// R-MAT scale 22, S=512: 3 blocks (80 registers, a few spills) 0.82 ms,
+// 2 blocks (113 registers) 0.96 ms, 4 blocks (64 registers) 0.92 ms.
+#define MSBFS_RED_MIN_BLOCKS 3
+#endif
+constexpr int RED_MIN_BLOCKS = MSBFS_RED_MIN_BLOCKS;
 constexpr uint32_t RED_CHUNK = 2048;  // vertices per reduction work item
 
 template <int VEC>
