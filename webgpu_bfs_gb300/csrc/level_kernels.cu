@@ -28,7 +28,10 @@
 
 namespace msbfs {
 
-constexpr int LEVEL_BLOCK = 256;
+#ifndef MSBFS_LEVEL_BLOCK
+#define MSBFS_LEVEL_BLOCK 256
+#endif
+constexpr int LEVEL_BLOCK = MSBFS_LEVEL_BLOCK;
 constexpr int BQ_CAP = 2048;  // discovered vertices staged per block
 #ifndef MSBFS_PULL_CH
 #define MSBFS_PULL_CH 4
@@ -38,7 +41,7 @@ constexpr int BQ_CAP = 2048;  // discovered vertices staged per block
 // the bottom-up gathers are latency-bound, and the extra warps outweigh the
 // spilled registers (R-MAT scale 22, S=512: dense levels 2.29 -> 1.92 ms
 // against 6 blocks at 40 registers; 4 and 5 blocks were slower still).
-#define MSBFS_LEVEL_MIN_BLOCKS 8
+#define MSBFS_LEVEL_MIN_BLOCKS (2048 / MSBFS_LEVEL_BLOCK)
 #endif
 constexpr int CH = MSBFS_PULL_CH;  // in-neighbours gathered per chunk
 constexpr int MAT_BLOCK = 256;
