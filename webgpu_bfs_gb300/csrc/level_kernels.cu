@@ -326,10 +326,11 @@ __device__ __forceinline__ bool in_frontier(const uint32_t* fb, uint32_t u) {
 }
 
 // Vertex tiles a warp claims per cursor bump: small batches even out the end
-// of a level (R-MAT scale 22, S=512, bottom-up time: 4 tiles 8% and 8 tiles
-// 6% below 16; 32 tiles 15% above).
+// of a level (R-MAT scale 22, S=512, 8 blocks per SM, slices of 512: a step
+// takes 8.59 ms with 2 tiles, 8.52 with 1, 8.83 with 4; at 6 blocks and
+// slices of 256, 4 tiles had been 8% and 8 tiles 6% below 16).
 #ifndef MSBFS_TILE_BATCH
-#define MSBFS_TILE_BATCH 4
+#define MSBFS_TILE_BATCH 2
 #endif
 constexpr uint32_t TILE_BATCH = MSBFS_TILE_BATCH;
 
