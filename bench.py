@@ -43,7 +43,7 @@ WORKLOADS = {
     # served form: a resident graph answering a Poisson stream of requests
     # with |S| drawn from {1, 8, 64, 512, 2048}, per-source statistics out
     "served_rmat24": dict(kind="served", graph=dict(kind="rmat", scale=24, ef=16, seed=24024),
-                          requests=160, seed=5150),
+                          requests=160, seed=5150, verify_sources=48),
     "served_road1448": dict(kind="served",
                             graph=dict(kind="road", w=1448, h=1448, extra=41934, seed=1448),
                             requests=240, seed=5151),
@@ -52,7 +52,7 @@ WORKLOADS = {
     # up to 512 lanes (no express split: all requests are small)
     "served_rmat22_small": dict(kind="served",
                                 graph=dict(kind="rmat", scale=22, ef=16, seed=20220),
-                                requests=400, seed=5152, sizes=(1, 8, 64),
+                                requests=400, seed=5152, sizes=(1, 8, 64), verify_sources=128,
                                 fractions=(0.3, 0.4, 0.5, 0.6, 0.8),
                                 server=dict(slots=2, express_slots=0, small_sources=64,
                                             general_sm_percent=100,
@@ -73,13 +73,14 @@ def make_graph(m, spec):
 
 
 def workload_config(name, spec, g):
+    """The `config` of a workload's JSON line; both arms print the same dict."""
     if spec["kind"] == "served":
         return {"workload": name, "graph": spec["graph"], "num_vertices": g.num_vertices,
                 "num_edges": g.num_edges, "requests": spec["requests"],
                 "request_sizes": list(spec.get("sizes", SERVED_SIZES))}
     cfg = {"workload": name, "num_vertices": g.num_vertices, "num_edges": g.num_edges,
            "sources": spec["S"], "source_sampling": "uniform among degree>=1, seeded",
-           "graph": spec["kind"]}
+           "graph": spec["kind"], "l2_policy": l2_policy(g, spec["S"])}
     if spec["kind"] == "rmat":
         cfg.update(scale=spec["scale"], edge_factor=spec["ef"], abcd=[0.57, 0.19, 0.19, 0.05])
     return cfg
@@ -167,25 +168,89 @@ def level_bytes(rec, V, W, E):
             + 4 * rec["new_pairs"])
 
 
-def cpu_sample_rate(oracle, g, sources, target_s=12.0, max_sources=None):
-    """Times the threaded FIFO oracle (all host cores) on a bounded sample of
-    the workload's sources; returns (sources/s, n_sampled, threads, seconds)."""
+def cpu_model() -> str:
+    """Host CPU model as lscpu (or /proc/cpuinfo) names it."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        names = [ln.split(":", 1)[1].strip() for ln in out.splitlines()
+                 if ln.strip().lower().startswith("model name")]
+        if names:
+            return " / ".join(dict.fromkeys(names))
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_sample_rate(oracle, g, sources, target_s=12.0, gpu_rows=None, max_sources=None):
+    """Times the threaded FIFO oracle (the reference's Rayon path restated,
+    all host cores) on consecutive chunks of the workload's sources until
+    about `target_s` seconds of CPU work are done. When `gpu_rows(i0, i1)` is
+    given, each chunk's oracle rows are compared byte for byte with the GPU's
+    rows of the same sources (outside the timed oracle calls). Returns
+    (sources/s, sources sampled, threads, seconds, parity dict or None)."""
     threads = os.cpu_count() or 1
-    n = min(len(sources), threads)
-    t0 = time.perf_counter()
-    oracle.ms_bfs_threaded(g.num_vertices, g.row_offsets, g.col_indices, sources[:n], threads)
-    dt = time.perf_counter() - t0
-    per = dt / n
-    more = int(max(0, target_s - dt) / max(per, 1e-9))
-    cap = max_sources if max_sources else len(sources)
-    n2 = min(cap - n, more) if cap > n else 0
-    if n2 > 0:
+    V = g.num_vertices
+    cap = min(len(sources), max_sources or len(sources))
+    done, secs = 0, 0.0
+    rows, mismatched_rows, bad_values = 0, 0, 0
+    first_bad = None
+    while done < cap and (done == 0 or secs < target_s):
+        n = min(threads, cap - done)
         t0 = time.perf_counter()
-        oracle.ms_bfs_threaded(g.num_vertices, g.row_offsets, g.col_indices,
-                               sources[n:n + n2], threads)
-        dt2 = time.perf_counter() - t0
-        return n2 / dt2, n2, threads, dt2
-    return n / dt, n, threads, dt
+        want = oracle.ms_bfs_threaded(V, g.row_offsets, g.col_indices,
+                                      sources[done:done + n], threads)
+        secs += time.perf_counter() - t0
+        if gpu_rows is not None:
+            for got in gpu_rows(done, done + n):
+                got = np.asarray(got).view(np.uint32).reshape(n, V)
+                w = want.reshape(n, V)
+                ne = got != w
+                nrow = int(ne.any(axis=1).sum())
+                if nrow and first_bad is None:
+                    r = int(np.flatnonzero(ne.any(axis=1))[0])
+                    v = int(np.flatnonzero(ne[r])[0])
+                    first_bad = {"source_index": done + r, "vertex": v,
+                                 "expected": int(w[r, v]), "got": int(got[r, v])}
+                mismatched_rows += nrow
+                bad_values += int(ne.sum())
+            rows += n
+        done += n
+    parity = None
+    if gpu_rows is not None:
+        parity = {"rows_compared": rows, "mismatched_rows": mismatched_rows,
+                  "mismatches": bad_values, "against": "oracle threaded FIFO rows",
+                  "first_mismatch": first_bad}
+    return done / secs, done, threads, secs, parity
+
+
+def cpu_fifo_single(oracle, g, sources, target_s=5.0):
+    """Times the single-thread FIFO oracle (crates/cpu_bfs/src/fifo.rs
+    restated) one source at a time for about `target_s` seconds; returns
+    (sources/s, sources timed, seconds)."""
+    n, secs = 0, 0.0
+    while n < len(sources) and (n == 0 or secs < target_s):
+        t0 = time.perf_counter()
+        oracle.ms_bfs_fifo(g.num_vertices, g.row_offsets, g.col_indices, sources[n:n + 1])
+        secs += time.perf_counter() - t0
+        n += 1
+    return n / secs, n, secs
+
+
+def l2_policy(g, S):
+    """The inputs of one step are larger than L2 (stated in the config)."""
+    W = 1
+    while W < min(16, (S + 31) // 32):
+        W *= 2
+    return "inputs larger than L2 (CSR %.2f GB, traversal state %.2f GB, %.2f GB of rows)" % (
+        (4 * (g.num_vertices + 1) + 4 * g.num_edges) / 1e9, W * 4 * g.num_vertices * 13 / 1e9,
+        4 * S * g.num_vertices / 1e9)
 
 
 def run_reference(args, spec):
@@ -229,6 +294,7 @@ def run_reference(args, spec):
     cfg = workload_config(args.workload, spec, g)
     metric = ("served MS-BFS sources/sec (Poisson request stream, per-source stats)"
               if spec["kind"] == "served" else "MS-BFS sources/sec")
+    f_rate, f_n, f_secs = cpu_fifo_single(oracle, g, src, target_s=min(5.0, args.cpu_seconds))
     out = {
         "metric": metric, "value": value, "unit": "sources/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -236,8 +302,13 @@ def run_reference(args, spec):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "impl": "reference", "config": cfg,
         "cpu_baseline": {"value": value, "unit": "sources/s", "cores": threads, "kind": "port",
+                         "cpu_model": cpu_model(),
                          "sample": f"{n} of the {len(src)} sources per step, threaded FIFO "
-                                   f"(cpu_bfs rayon_ms.rs restated in C)"},
+                                   f"(cpu_bfs rayon_ms.rs restated in C)",
+                         "fifo_single": {"value": f_rate, "unit": "sources/s", "cores": 1,
+                                         "sample": f"{f_n} sources one at a time in "
+                                                   f"{f_secs:.1f} s, single-thread FIFO "
+                                                   f"(cpu_bfs fifo.rs restated in C)"}},
         "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -391,6 +462,7 @@ def run_ours(args, spec):
 
     # ---- e2e: host API, pinned host sources in, full distance matrix out
     e2e = None
+    host_out = None
     try:
         host_out = torch.empty(S * V, dtype=torch.int32, pin_memory=True)
         host_src = torch.from_numpy(src.astype(np.int32)).pin_memory()
@@ -412,19 +484,40 @@ def run_ours(args, spec):
                "ms_per_step": 1000 * dt / args.steps,
                "note": "graph resident (uploaded once); per step: sources H2D, BFS, "
                        "S*V u32 distances D2H into pinned host memory"}
-        del host_out
     except Exception as ex:  # pragma: no cover - reported, not hidden
         e2e = {"value": None, "unit": "sources/s", "error": repr(ex)[:200]}
 
-    # ---- CPU baseline (rank 0, N=1 only)
+    # ---- CPU baseline (rank 0, N=1 only) and bit-exact parity: the oracle
+    # rows the baseline computes are compared with the same sources' rows of
+    # the timed device run (`out`) and of the host-API run (`host_out`).
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle
         oracle.build()
-        rate, n, threads, secs = cpu_sample_rate(oracle, g, src, target_s=args.cpu_seconds)
+
+        def gpu_rows(i0, i1):
+            rows = [out[i0 * V:i1 * V].cpu().numpy()]
+            if host_out is not None and e2e.get("value") is not None:
+                rows.append(host_out[i0 * V:i1 * V].numpy())
+            return rows
+
+        rate, n, threads, secs, parity = cpu_sample_rate(oracle, g, src,
+                                                         target_s=args.cpu_seconds,
+                                                         gpu_rows=gpu_rows)
+        parity["paths"] = ["device output of the timed run"] + (
+            ["host-API output of the e2e run"] if host_out is not None and
+            e2e.get("value") is not None else [])
+        f_rate, f_n, f_secs = cpu_fifo_single(oracle, g, src[n:] if n < S else src,
+                                              target_s=min(5.0, args.cpu_seconds))
         cpu = {"value": rate, "unit": "sources/s", "cores": threads, "kind": "port",
+               "cpu_model": cpu_model(),
                "sample": f"{n} of the {S} sources, threaded FIFO (cpu_bfs rayon_ms.rs "
-                         f"restated in C), {secs:.1f} s"}
+                         f"restated in C), {secs:.1f} s",
+               "fifo_single": {"value": f_rate, "unit": "sources/s", "cores": 1,
+                               "sample": f"{f_n} sources one at a time in {f_secs:.1f} s, "
+                                         f"single-thread FIFO (cpu_bfs fifo.rs restated in C)"}}
+    del host_out
 
     if rank == 0:
         res = {
@@ -432,14 +525,12 @@ def run_ours(args, spec):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": max_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": dict(workload_config(args.workload, spec, g),
-                           l2_policy="inputs larger than L2 (CSR %.2f GB, state %.2f GB)" % (
-                               (4 * (V + 1) + 4 * g.num_edges) / 1e9,
-                               (st["words_per_vertex"] * 4 * V * 13) / 1e9),
-                           method=int(st["method"]), path=int(st["path"]),
-                           words_per_vertex=st["words_per_vertex"], passes=st["passes"],
-                           levels=st["levels"], push_levels=st["push_levels"],
-                           pull_levels=st["pull_levels"], parallelism=f"replicas x{world}"),
+            "config": workload_config(args.workload, spec, g),
+            "engine": {"method": int(st["method"]), "path": int(st["path"]),
+                       "words_per_vertex": st["words_per_vertex"], "passes": st["passes"],
+                       "levels": st["levels"], "push_levels": st["push_levels"],
+                       "pull_levels": st["pull_levels"], "parallelism": f"replicas x{world}"},
+            "parity": parity,
             "gteps": gteps, "traversed_edges_per_step": tedges,
             "p50_ms": statistics.median(step_ms),
             "p99_ms": float(np.percentile(step_ms, 99)),
@@ -459,6 +550,24 @@ def run_ours(args, spec):
     eng.close()
     if world > 1:
         dist.destroy_process_group()
+    if rank == 0 and parity_failed(res):
+        print("bit-exact parity check failed", file=sys.stderr)
+        sys.exit(3)
+
+
+def parity_failed(res) -> bool:
+    """True when any parity record in the line counted a mismatch."""
+    bad = False
+    if isinstance(res, dict):
+        for k, v in res.items():
+            if k == "parity" and isinstance(v, dict) and v.get("mismatches"):
+                bad = True
+            elif isinstance(v, (dict, list)):
+                bad |= parity_failed(v)
+    elif isinstance(res, list):
+        for v in res:
+            bad |= parity_failed(v)
+    return bad
 
 
 def make_batch(m, spec):
@@ -485,9 +594,11 @@ def make_batch(m, spec):
     return items
 
 
-def batched_experiment(m, spec, steps, warmup):
+def batched_experiment(m, spec, steps, warmup, verify_stride=10):
     """Batched form (one persistent launch over every graph) vs the plain
-    per-graph launch loop, both device-timed."""
+    per-graph launch loop, both device-timed. Afterwards every
+    `verify_stride`-th graph's rows from the last batched launch are compared
+    byte for byte with the threaded FIFO oracle."""
     t0 = time.perf_counter()
     items = make_batch(m, spec)
     gen_s = time.perf_counter() - t0
@@ -499,18 +610,33 @@ def batched_experiment(m, spec, steps, warmup):
         for _ in range(max(1, warmup)):
             b.run()
             b.run_per_graph()
+        plain = [b.run_per_graph() for _ in range(steps)]
         with ClockSampler(0) as clk:
             batched = [b.run() for _ in range(steps)]
-        plain = [b.run_per_graph() for _ in range(steps)]
         classes = {}
         for i in range(len(items)):
             c = b.config(i)
             classes[c["class"]] = {k: c[k] for k in ("alg", "words", "param")}
+        parity = None
+        if verify_stride:
+            from oracle import oracle
+            oracle.build()
+            graphs = rows = bad = 0
+            for i in range(0, len(items), verify_stride):
+                g, src = items[i]
+                want = oracle.ms_bfs_threaded(g.num_vertices, g.row_offsets, g.col_indices,
+                                              src)
+                got = b.result(i)
+                bad += int(np.count_nonzero(got != want))
+                graphs += 1
+                rows += int(src.size)
+            parity = {"graphs_compared": graphs, "rows_compared": rows, "mismatches": bad,
+                      "against": "oracle threaded FIFO rows, every %d-th graph" % verify_stride}
     finally:
         b.close()
     return {"items": items, "batched_ms": batched, "plain_ms": plain, "gen_s": gen_s,
             "tune_s": tune_s, "classes": classes, "clocks": clk.summary(),
-            "sources": sum(int(s.size) for _, s in items),
+            "sources": sum(int(s.size) for _, s in items), "parity": parity,
             "vertices": sum(g.num_vertices for g, _ in items)}
 
 
@@ -535,9 +661,13 @@ def run_batched(args, spec):
         "speedup_vs_plain": ms_p / ms_b,
         "p50_ms": ms_b, "p99_ms": float(np.percentile(r["batched_ms"], 99)),
         "clocks": r["clocks"],
+        "parity": r["parity"],
         "gpu_launches": 1,
     }
     print(json.dumps(res), flush=True)
+    if parity_failed(res):
+        print("bit-exact parity check failed", file=sys.stderr)
+        sys.exit(3)
 
 
 def forms_summary(g_rmat22=None):
@@ -556,7 +686,7 @@ def forms_summary(g_rmat22=None):
         g = g_rmat22 if g_rmat22 is not None else make_graph(m, spec["graph"])
         reqs = make_requests(g, 240, spec["seed"], spec["sizes"])
         r = served_experiment(m, g, reqs, spec["server"], fractions=(0.4, 0.5),
-                              seed=spec["seed"], warm=20)
+                              seed=spec["seed"], warm=20, verify_sources=96)
         out["served_small"] = {
             "workload": "served_rmat22_small (240 requests of 1, 8 or 64 sources)",
             "sources_per_s": r["served_capacity"],
@@ -568,6 +698,7 @@ def forms_summary(g_rmat22=None):
                             "served": p["served"], "plain": p["plain"]} for p in r["sweep"]],
             "latency_alone_ms": r["latency_alone_ms"],
             "identical_results": f"{r['identical_results']}/{r['compared_results']}",
+            "parity": r["parity"],
             "kernel_launches": r["kernel_launches"]}
     except Exception as ex:  # reported, not hidden
         out["served_small"] = {"error": repr(ex)[:300]}
@@ -576,7 +707,8 @@ def forms_summary(g_rmat22=None):
         mb, mp = statistics.median(r["batched_ms"]), statistics.median(r["plain_ms"])
         out["batched"] = {"workload": "batched1000", "sources_per_s": r["sources"] / mb * 1e3,
                           "plain_sources_per_s": r["sources"] / mp * 1e3,
-                          "speedup_vs_plain": mp / mb, "ms": mb, "plain_ms": mp}
+                          "speedup_vs_plain": mp / mb, "ms": mb, "plain_ms": mp,
+                          "parity": r["parity"]}
     except Exception as ex:  # reported, not hidden
         out["batched"] = {"error": repr(ex)[:300]}
     try:
@@ -584,7 +716,7 @@ def forms_summary(g_rmat22=None):
         g = make_graph(m, spec["graph"])
         reqs = make_requests(g, 120, spec["seed"])
         r = served_experiment(m, g, reqs, SERVED_CONFIG, fractions=(0.5,), seed=spec["seed"],
-                              warm=20)
+                              warm=20, verify_sources=512)
         pt = r["sweep"][0]
         out["served"] = {
             "workload": "served_road1448 (120 requests)",
@@ -594,6 +726,7 @@ def forms_summary(g_rmat22=None):
             "at_half_load": {"served": pt["served"], "plain": pt["plain"]},
             "latency_alone_ms": r["latency_alone_ms"],
             "identical_results": f"{r['identical_results']}/{r['compared_results']}",
+            "parity": r["parity"],
             "kernel_launches": r["kernel_launches"]}
     except Exception as ex:  # reported, not hidden
         out["served"] = {"error": repr(ex)[:300]}
@@ -681,10 +814,40 @@ def plain_stream(eng, g, reqs, arrivals):
     return outs, lat, t_end - (t0 + arrivals[0])
 
 
-def served_experiment(m, g, reqs, cfg, fractions=(0.3, 0.6, 0.9), seed=0, warm=40):
+def oracle_stats(oracle, g, src):
+    """Per-source eccentricity / reached count / distance sum from the
+    threaded FIFO oracle's rows."""
+    V = g.num_vertices
+    d = oracle.ms_bfs_threaded(V, g.row_offsets, g.col_indices, src).reshape(len(src), V)
+    fin = d != 0xFFFFFFFF
+    dz = np.where(fin, d, 0)
+    return dz.max(1).astype(np.uint32), fin.sum(1).astype(np.uint32), dz.sum(1, dtype=np.uint64)
+
+
+def served_parity(oracle, g, reqs, outs, source_budget):
+    """Compares served per-source statistics with the oracle's for requests
+    taken in arrival order until `source_budget` sources are covered."""
+    n_req = n_src = bad = 0
+    for r, o in zip(reqs, outs):
+        if n_src and n_src + r.size > source_budget:
+            continue
+        ecc, reached, dsum = oracle_stats(oracle, g, r)
+        bad += int(np.count_nonzero(o["eccentricity"] != ecc))
+        bad += int(np.count_nonzero(o["reached"] != reached))
+        bad += int(np.count_nonzero(o["distance_sum"] != dsum))
+        n_req += 1
+        n_src += int(r.size)
+    return {"requests_compared": n_req, "sources_compared": n_src, "mismatches": bad,
+            "against": "per-source statistics of oracle threaded FIFO rows"}
+
+
+def served_experiment(m, g, reqs, cfg, fractions=(0.3, 0.6, 0.9), seed=0, warm=40,
+                      verify_sources=256):
     """Capacity (all requests at t=0) of the served form and of the plain
     path, then Poisson streams offered at fractions of the served capacity
-    through both. Every served result is compared with the plain one."""
+    through both. Every served result is compared with the plain one, and
+    the served results of the saturated run for up to `verify_sources`
+    sources with the oracle's."""
     import torch
     sizes = [int(r.size) for r in reqs]
     total = float(sum(sizes))
@@ -726,7 +889,13 @@ def served_experiment(m, g, reqs, cfg, fractions=(0.3, 0.6, 0.9), seed=0, warm=4
                           "served": dict(_latency_summary(sl, sizes),
                                          sources_per_s=total / ss),
                           "plain": dict(_latency_summary(pl, sizes), sources_per_s=total / ps)})
+        parity = None
+        if verify_sources:
+            from oracle import oracle
+            oracle.build()
+            parity = served_parity(oracle, g, reqs, s_out, verify_sources)
         return {
+            "parity": parity,
             "served_capacity": cap_s, "plain_capacity": cap_p,
             "served_saturated": dict(_latency_summary(s_lat, sizes), makespan_s=s_span),
             "plain_saturated": dict(_latency_summary(p_lat, sizes), makespan_s=p_span),
@@ -757,7 +926,7 @@ def run_served(args, spec):
     reqs = make_requests(g, spec["requests"], spec["seed"], sizes)
     total = sum(int(r.size) for r in reqs)
     r = served_experiment(m, g, reqs, cfg, fractions=spec.get("fractions", (0.3, 0.6, 0.9)),
-                          seed=spec["seed"])
+                          seed=spec["seed"], verify_sources=spec.get("verify_sources", 256))
     ok = [p for p in r["sweep"] if p["served"]["small_p99_ms"] is not None
           and p["served"]["small_p99_ms"] <= 20.0]
     sat = r["served_saturated"]
@@ -781,8 +950,9 @@ def run_served(args, spec):
         "latency_alone_ms": r["latency_alone_ms"],
         "best_sources_per_s_with_small_p99_le_20ms":
             max((p["served"]["sources_per_s"] for p in ok), default=None),
-        "parity": f"{r['identical_results']}/{r['compared_results']} served results "
-                  f"identical to the plain path",
+        "served_vs_plain": f"{r['identical_results']}/{r['compared_results']} served results "
+                           f"identical to the plain path",
+        "parity": r["parity"],
         "e2e": {"value": r["served_capacity"], "unit": "sources/s",
                 "h2d_bytes_per_step": int(4 * total / len(reqs)),
                 "d2h_bytes_per_step": int(16 * total / len(reqs)),
@@ -792,6 +962,9 @@ def run_served(args, spec):
         "gpu_launches": r["kernel_launches"],
     }
     print(json.dumps(res), flush=True)
+    if parity_failed(res):
+        print("bit-exact parity check failed", file=sys.stderr)
+        sys.exit(3)
 
 
 def run_ncu_case(args, spec):

@@ -157,6 +157,17 @@ int msbfs_engine_set_tuning(msbfs_engine *engine, uint32_t max_words_per_pass,
  * slots). No reference counterpart. Results do not depend on it. */
 int msbfs_engine_set_sm_share(msbfs_engine *engine, uint32_t percent);
 
+/* Caps the levels of one level-synchronous pass (0, the default, = V + 2,
+ * which no traversal reaches). A pass still running at the cap stops, its
+ * buffers are cleared as after a normal stop, and the call returns
+ * MSBFS_ERR_TIMEOUT ("level cap reached"); the engine stays usable. The
+ * reference bounds its hop loop at V hops and, if that runs out, returns the
+ * rows it has without an error (crates/gpu_bfs/src/dispatch/
+ * indirect_sparse_push.rs:1463-1577); here partial rows are never reported as
+ * a success. The CTA-per-source path ends after at most V levels by
+ * construction and ignores the cap. */
+int msbfs_engine_set_level_cap(msbfs_engine *engine, uint32_t max_levels);
+
 /* Profiling: 0 off; 1 keep a per-level record of every call (device timers,
  * the level loop stays on the device); 2 as 1, but the level loop is driven
  * from the host one launch at a time with CUDA events around each launch.
@@ -313,32 +324,41 @@ int msbfs_traversed_edges_device(msbfs_engine *engine, const msbfs_graph *graph,
 /* ------------------------------------------------------------------------
  * Multi-source BFS that allocates nothing. No counterpart in the reference.
  *
- * For callers that cannot call cudaMalloc: code that runs while a CUDA stream
- * capture is active on the device (the allocator may not be used then), hosts
- * that hand all device memory to their own pool and forbid allocations from
- * libraries, and long-running services that reserve their memory up front.
+ * For callers that must not call cudaMalloc: host applications that hand all
+ * device memory to their own pool allocator and do not let libraries
+ * allocate beside it, and services that reserve every byte they will use
+ * when they start, so that no request can fail later for want of memory.
  * Every other entry point allocates engine-owned device buffers; this one
  * uses no engine. It runs the one-block-per-source BFS (the kernel behind
  * MSBFS_METHOD_WORKGROUP_PERSISTENT_BFS) with its scratch -- a copy of the
- * sources, the source cursor and one frontier queue of 2*V u32 per resident
- * block -- in a fixed device array of MSBFS_NOALLOC_SCRATCH_BYTES inside the
- * library. Every GPU that loads the library holds that array until exit.
+ * sources, the source cursor and one frontier queue slab of V u32 per
+ * resident block -- in a fixed device array of MSBFS_NOALLOC_SCRATCH_BYTES
+ * inside the library. Every GPU that loads the library holds that array
+ * until the process exits.
  *
  * Inputs and outputs stay the caller's: the CSR arrays and the S*V u32
  * distance matrix are DEVICE pointers (dist[s*V + v], unreachable =
  * 0xFFFFFFFF, the same bytes as msbfs_run_ms_bfs); `sources` is a HOST array,
  * validated like msbfs_run_ms_bfs (MSBFS_ERR_SOURCE_OOB) and copied into the
- * fixed array. Work is queued on `cuda_stream` (NULL = legacy default stream)
- * and the call returns without waiting. Graphs with more than
- * MSBFS_NOALLOC_MAX_VERTICES vertices are rejected with
+ * fixed array with cudaMemcpyAsync on `cuda_stream`: from pageable memory the
+ * copy is staged before the call returns, from page-locked memory it runs in
+ * stream order, so such an array must stay unchanged until the stream has
+ * passed this call. Work is queued on `cuda_stream` (NULL = legacy default
+ * stream) and the call returns without waiting. Calls of more than 65,536
+ * sources run as consecutive chunks of at most that many. Graphs with more
+ * than MSBFS_NOALLOC_MAX_VERTICES vertices are rejected with
  * MSBFS_ERR_SCRATCH_TOO_SMALL before anything is queued.
  *
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
- * capture begins. All calls share the one array, which keeps the last call's
- * contents (the cursor is cleared by each call): calls that overlap on the
- * GPU -- on different streams, or before the previous call's work finished
- * on another stream -- race on it and must be serialised by the caller. */
+ * capture begins. The calling thread's current device is restored before
+ * the call returns, and a CUDA error left pending on the thread by earlier
+ * work is cleared before this call queues its own, so MSBFS_ERR_CUDA reports
+ * this call's failures only. All calls share the one array, which keeps the
+ * last call's contents (the cursor is cleared by each call): calls that
+ * overlap on the GPU -- on different streams, or before the previous call's
+ * work finished on another stream -- race on it and must be serialised by
+ * the caller. */
 #define MSBFS_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define MSBFS_NOALLOC_MAX_VERTICES 1048576u
 int msbfs_run_cta_noalloc(int device, size_t num_vertices,

@@ -293,3 +293,42 @@ def test_cta_frontier_beyond_shared_queue(native, oracle):
             assert_same(got, _oracle(oracle, g, src), g, src, f"CTA V={g.num_vertices}")
     finally:
         eng.close()
+
+
+@pytest.mark.parametrize("loop", ["graph", "host"])
+def test_level_cap_times_out_and_engine_recovers(native, oracle, monkeypatch, loop):
+    """A pass still running at the level cap stops with MSBFS_ERR_TIMEOUT
+    (code 4) through the CUDA-graph WHILE loop and through the host-driven
+    loop. Its buffers are left clean -- the frontier it was about to expand
+    included -- so a following call on the same workspace (same graph and
+    word width) whose traversal ends under the cap is bit-exact. The graph is
+    a path of 1,500 vertices (1,499 levels) beside a star of 11 vertices."""
+    if loop == "host":
+        monkeypatch.setenv("MSBFS_HOST_LOOP", "1")
+    edges = [(i, i + 1) for i in range(1499)] + [(1500, 1501 + k) for k in range(10)]
+    edges += [(b, a) for a, b in edges]
+    g = native.CsrGraph.from_edge_list(1511, edges)
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.PushPullAdaptive)
+    try:
+        deep = np.array([0, 1499, 700, 3], np.uint32)
+        star = np.array([1500, 1505, 1501, 1509], np.uint32)
+        # Stopped at level 8, the pass leaves level 9's frontier in rotation
+        # slot 0, which the next pass's first bottom-up level reads without a
+        # frontier-bitmap filter: left uncleared, its path vertices would
+        # hand the star's lanes distances on the path.
+        eng.set_level_cap(9)
+        for method in ("MultiWordBitParallel", "PushPullAdaptive"):
+            m = native.GpuBfsMethod[method]
+            for _ in range(2):
+                with pytest.raises(native.BfsError) as ei:
+                    eng.run_ms_bfs_with_method(m, g, deep)
+                assert ei.value.code == 4 and "level cap" in str(ei.value)
+                assert_same(eng.run_ms_bfs_with_method(m, g, star), _oracle(oracle, g, star),
+                            g, star, f"{loop} loop, {method}: same workspace after the cap")
+        eng.set_level_cap(0)
+        want = _oracle(oracle, g, deep)
+        for method in ("PushPullAdaptive", "MultiWordBitParallel", "BitParallel64"):
+            got = eng.run_ms_bfs_with_method(native.GpuBfsMethod[method], g, deep)
+            assert_same(got, want, g, deep, f"{loop} loop after the cap, {method}")
+    finally:
+        eng.close()

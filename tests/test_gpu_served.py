@@ -147,8 +147,12 @@ def test_sm_share_same_results(native, oracle):
         eng.close()
 
 
-def test_server_wait_timeout_and_empty(native):
-    g = native.generate_graph500_rmat(10, 8, 5)
+def test_server_wait_timeout_and_empty(native, oracle):
+    """A wait whose limit runs out returns MSBFS_ERR_TIMEOUT (code 4) and
+    keeps the ticket; a later wait returns the result. The request (2,048
+    distance rows on a road graph of ~1,000 levels) takes milliseconds, the
+    first wait's limit is 10 microseconds."""
+    g = native.wilson_grid(339, 338, 5000, 1442)
     srv = native.BfsServer(g, slots=1)
     try:
         t = srv.submit(np.zeros(0, np.uint32), srv.STATS)
@@ -156,5 +160,14 @@ def test_server_wait_timeout_and_empty(native):
         assert res.size == 0 and info["launches"] == 0
         with pytest.raises(native.BfsError):
             srv.submit(np.array([g.num_vertices], np.uint32), srv.STATS)
+        src = native.sample_sources(g, 2048, 7)
+        t = srv.submit(src, srv.ROWS)
+        with pytest.raises(native.BfsError) as ei:
+            srv.wait(t, timeout_ms=0.01)
+        assert ei.value.code == 4
+        res, info = srv.wait(t)
+        assert info["status"] == 0 and info["latency_ms"] > 0.01
+        want = oracle.ms_bfs_threaded(g.num_vertices, g.row_offsets, g.col_indices, src)
+        assert_same(res, want, g, src, "rows after an expired wait")
     finally:
         srv.close()

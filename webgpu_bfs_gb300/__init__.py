@@ -403,6 +403,11 @@ class GpuBfsEngine:
         self._check(_native.lib().msbfs_engine_set_tuning(self._h, max_words_per_pass, alpha,
                                                           beta))
 
+    def set_level_cap(self, max_levels: int) -> None:
+        """Stops a level-synchronous pass after ``max_levels`` levels with
+        BfsError code 4 (Timeout); 0 restores the default (V + 2)."""
+        self._check(_native.lib().msbfs_engine_set_level_cap(self._h, int(max_levels)))
+
     def set_profiling(self, level: int) -> None:
         """0 off, 1 per-level records (device timers), 2 records + host-driven
         level loop with CUDA events around every launch."""

@@ -128,6 +128,7 @@ SIGNATURES = {
     "msbfs_engine_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "msbfs_engine_set_tuning": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]),
     "msbfs_engine_set_sm_share": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "msbfs_engine_set_level_cap": (C.c_int, [C.c_void_p, C.c_uint32]),
     "msbfs_engine_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "msbfs_engine_level_log": (C.c_int, [C.c_void_p, C.POINTER(LevelRecord), C.c_size_t,
                                          sizep]),

@@ -605,6 +605,24 @@ uint32_t* g_noalloc_addr[64];  // device address of the array, per device
 
 }  // namespace msbfs
 
+namespace {
+
+// Restores the calling thread's current device when the entry point returns.
+struct DeviceRestore {
+  int prev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+  }
+  ~DeviceRestore() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
 extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
                                      const uint32_t* row_offsets_device,
                                      const uint32_t* col_indices_device,
@@ -623,6 +641,7 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
   if (num_vertices > MSBFS_NOALLOC_MAX_VERTICES ||
       NOALLOC_Q_OFF + num_vertices > NOALLOC_WORDS)
     return MSBFS_ERR_SCRATCH_TOO_SMALL;
+  const DeviceRestore restore;
   if (cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
     return MSBFS_ERR_NO_DEVICE;
@@ -650,9 +669,14 @@ extern "C" int msbfs_run_cta_noalloc(int device, size_t num_vertices,
     return MSBFS_ERR_SCRATCH_TOO_SMALL;
   const size_t slabs = (NOALLOC_WORDS - NOALLOC_Q_OFF) / (size_t)V;
   const cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  // A non-sticky error left on this thread by earlier work would otherwise
+  // be reported as this call's launch failure below.
+  cudaGetLastError();
   for (size_t s0 = 0; s0 < num_sources; s0 += NOALLOC_SRC_CAP) {
     const size_t n = std::min(NOALLOC_SRC_CAP, num_sources - s0);
-    // The cursor must start at zero; queue slabs need no clearing.
+    // The cursor must start at zero; queue slabs need no clearing. Chunks
+    // follow one another in stream order, so a chunk's copy of its sources
+    // cannot overwrite those of the chunk before it while that one runs.
     if (cudaMemsetAsync(base, 0, sizeof(uint32_t), s) != cudaSuccess ||
         cudaMemcpyAsync(base + NOALLOC_SRC_OFF, sources + s0, n * sizeof(uint32_t),
                         cudaMemcpyHostToDevice, s) != cudaSuccess) {

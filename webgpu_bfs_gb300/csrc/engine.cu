@@ -80,6 +80,10 @@ struct Workspace {
   PassDesc* d_desc = nullptr;
   LevelRec* d_log = nullptr;
   std::vector<void*> allocs;
+  // Set when a pass stopped part-way (an error after work was queued): its
+  // buffers may hold that pass's bits, so the next call builds a fresh
+  // workspace instead of reusing this one.
+  bool dirty = false;
   // One instantiated pass per finishing kernel: [0] materialise, [1] reduce
   // (built on first use).
   cudaGraph_t graph[2] = {nullptr, nullptr};
@@ -149,6 +153,7 @@ struct msbfs_engine {
   uint32_t split = MSBFS_SPLIT;  // in-edge slice length of bottom-up steps
   uint32_t bits_div = 64;
   uint32_t sm_share = 100;  // percent of the resident grid the persistent kernels use
+  uint32_t level_cap = 0;   // levels per pass before MSBFS_ERR_TIMEOUT (0: V + 2)
   bool host_loop = false;
   bool zero_copy = true;  // MSBFS_ZERO_COPY=0 stages host output in HBM instead
   int profiling = 0;
@@ -323,8 +328,13 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   auto key = std::make_tuple(g->id, W, mode);
   auto it = eng->ws.find(key);
   if (it != eng->ws.end()) {
-    *out = it->second.get();
-    return MSBFS_OK;
+    if (!it->second->dirty) {
+      *out = it->second.get();
+      return MSBFS_OK;
+    }
+    CK(cudaStreamSynchronize(eng->stream));
+    CK(cudaStreamSynchronize(eng->copy_stream));
+    eng->ws.erase(it);
   }
   // One pooled workspace per graph: drop any other (W, mode) of this graph
   // only if memory runs short (allocation failure below retries once).
@@ -362,6 +372,7 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   p.heavy = eng->heavy;
   p.bits_div = eng->bits_div;
   p.max_levels = (uint32_t)std::min<uint64_t>(g->V + 2, 0xFFFFFFF0ull);
+  if (eng->level_cap) p.max_levels = std::min(p.max_levels, eng->level_cap);
   p.split = g->split;
   p.n_hchunks = g->n_hchunks;
   p.hchunks = g->hchunks;
@@ -454,7 +465,10 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, bool reduce, std::vector<
     cudaEventElapsedTime(&t, eng->lvl_events[0], eng->lvl_events[1]);
     ms->push_back(t);
     if (probe.terminated) break;
-    if (L > w->p.max_levels) return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
+    if (L > w->p.max_levels) {
+      w->dirty = true;
+      return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
+    }
   }
   CK(cudaEventRecord(eng->lvl_events[0], eng->stream));
   launch_materialize(w->p, w->k, reduce, eng->stream);
@@ -483,8 +497,10 @@ int run_pass_host_loop(msbfs_engine* eng, Workspace* w, bool reduce) {
     CK(cudaMemcpyAsync(&probe, w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost, eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
     if (probe.terminated) break;
-    if (launched > (uint64_t)w->p.max_levels + 16)
+    if (launched > (uint64_t)w->p.max_levels + 16) {
+      w->dirty = true;
       return set_err(eng, MSBFS_ERR_TIMEOUT, "level loop did not terminate");
+    }
   }
   launch_materialize(w->p, w->k, reduce, eng->stream);
   launch_cleanup(w->p, eng->stream);
@@ -640,6 +656,9 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     eng->pass_event_ms.assign(passes, {});
   }
   const size_t wpv = (S + 31) / 32;
+  // Any early return below leaves passes half-queued: the workspace is
+  // retired unless the loop completes.
+  w->dirty = true;
   for (size_t ps = 0; ps < passes; ++ps) {
     const size_t s0 = ps * PW;
     const size_t np = std::min(PW, S - s0);
@@ -673,6 +692,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
                          cudaMemcpyDeviceToHost, eng->copy_stream));
     }
   }
+  w->dirty = false;
   if (host_reach) {
     CK(cudaMemcpyAsync(host_reach, reach_dev, V * wpv * sizeof(uint32_t),
                        cudaMemcpyDeviceToHost, eng->stream));
@@ -1003,6 +1023,16 @@ int msbfs_engine_set_sm_share(msbfs_engine* e, uint32_t percent) {
   cudaSetDevice(e->device);
   cudaStreamSynchronize(e->stream);
   e->ws.clear();  // grid sizes are baked into the captured graphs
+  return MSBFS_OK;
+}
+
+int msbfs_engine_set_level_cap(msbfs_engine* e, uint32_t max_levels) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->level_cap = max_levels;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->stream);
+  e->ws.clear();  // the cap is baked into the captured graphs
   return MSBFS_OK;
 }
 

@@ -1246,19 +1246,23 @@ size_t materialize_smem_bytes(uint32_t W, uint32_t NP) {
   return (size_t)(1 + np) * tw * (tv + 2) * sizeof(uint32_t);
 }
 
-// Zeroes the last frontier (level L_end) after the loop has stopped.
+// Zeroes the frontier rows left after the loop has stopped: those of the
+// last expanded level L and, when the level cap stopped a traversal that was
+// still going, those of level L + 1 (empty after a normal stop).
 template <int W>
 __global__ void cleanup_kernel(LevelParams p) {
   const uint32_t L = p.ctl->level;
-  const uint32_t sl = L % 3;
-  const uint32_t n = p.ctl->qcount[sl];
-  const unsigned long long* Qs = p.Q[sl];
-  uint32_t* Fs = p.F[sl];
-  const size_t total = (size_t)n * W;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const unsigned long long ent = Qs[i / W];
-    if ((ent >> 32) == 0) Fs[(size_t)(uint32_t)ent * W + i % W] = 0;
+  for (uint32_t k = 0; k < 2; ++k) {
+    const uint32_t sl = (L + k) % 3;
+    const uint32_t n = p.ctl->qcount[sl];
+    const unsigned long long* Qs = p.Q[sl];
+    uint32_t* Fs = p.F[sl];
+    const size_t total = (size_t)n * W;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const unsigned long long ent = Qs[i / W];
+      if ((ent >> 32) == 0) Fs[(size_t)(uint32_t)ent * W + i % W] = 0;
+    }
   }
 }
 
