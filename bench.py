@@ -426,13 +426,27 @@ def run_ours(args, spec):
     mat = None
     peak, peak_kind = load_peaks()
     if st["path"] != 4:
-        eng.set_profiling(2)
+        # Work counts from the level kernels' counting form (the loop on the
+        # device), durations from the production form launched one level at
+        # a time between CUDA events; the traversal is deterministic, so the
+        # two runs match level for level.
+        eng.set_profiling(1)
+        step()
+        eng.synchronize()
+        counts = {(r["pass"], r["level"]): r for r in eng.level_log() if r["dir"] in (0, 1)}
+        eng.set_profiling(3)
         step()
         eng.synchronize()
         recs = eng.level_log()
         eng.set_profiling(0)
         W = st["words_per_vertex"]
-        lv = [r for r in recs if r["dir"] in (0, 1)]
+        lv = []
+        for r in recs:
+            if r["dir"] not in (0, 1):
+                continue
+            c = counts[(r["pass"], r["level"])]
+            assert c["dir"] == r["dir"] and c["new_pairs"] == r["new_pairs"]
+            lv.append(dict(c, event_ms=r["event_ms"]))
         mt = [r for r in recs if r["dir"] == 2]
         tot_b = sum(level_bytes(r, V, W, g.num_edges) for r in lv)
         tot_ms = sum(r["event_ms"] for r in lv)

@@ -168,10 +168,14 @@ int msbfs_engine_set_sm_share(msbfs_engine *engine, uint32_t percent);
  * construction and ignores the cap. */
 int msbfs_engine_set_level_cap(msbfs_engine *engine, uint32_t max_levels);
 
-/* Profiling: 0 off; 1 keep a per-level record of every call (device timers,
- * the level loop stays on the device); 2 as 1, but the level loop is driven
- * from the host one launch at a time with CUDA events around each launch.
- * msbfs_engine_level_log copies the last call's records. */
+/* Profiling: 0 off; 1 keep a per-level record of every call (device timers
+ * and the work counters of the algorithmic-bytes model; the level loop stays
+ * on the device and runs the level kernels' counting form); 2 as 1, but the
+ * level loop is driven from the host one launch at a time with CUDA events
+ * around each launch; 3 as 2 with the production level kernels, which keep
+ * no work counters (the records carry durations, frontier sizes and
+ * discovered pairs only). msbfs_engine_level_log copies the last call's
+ * records. */
 int msbfs_engine_set_profiling(msbfs_engine *engine, int level);
 int msbfs_engine_level_log(const msbfs_engine *engine, msbfs_level_record *out,
                            size_t capacity, size_t *count);

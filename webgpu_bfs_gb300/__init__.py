@@ -409,8 +409,9 @@ class GpuBfsEngine:
         self._check(_native.lib().msbfs_engine_set_level_cap(self._h, int(max_levels)))
 
     def set_profiling(self, level: int) -> None:
-        """0 off, 1 per-level records (device timers), 2 records + host-driven
-        level loop with CUDA events around every launch."""
+        """0 off, 1 per-level records with work counters (device timers), 2
+        records + host-driven level loop with CUDA events around every launch,
+        3 as 2 with the production kernels (durations, no work counters)."""
         self._check(_native.lib().msbfs_engine_set_profiling(self._h, int(level)))
 
     def level_log(self) -> list:

@@ -153,12 +153,12 @@ struct LevelParams {
 // Launch helpers implemented in level_kernels.cu / cta_kernel.cu.
 struct LevelKernelInfo {
   void* init;         // kernel symbols for graph nodes
-  void* level;
+  void* level[2][2];  // [direction: DIR_PUSH, DIR_PULL][with profiling counters]
+  int level_grids[2]; // resident grid per direction
   void* materialize;
   void* reduce;       // per-source reductions in place of materialize
   void* cleanup;
   int level_block;
-  int level_grid;
   int mat_block;
   int mat_grid;
   size_t mat_smem;
@@ -170,7 +170,12 @@ struct LevelKernelInfo {
 bool level_kernel_info(uint32_t W, uint32_t NP, int num_sms, LevelKernelInfo* out);
 size_t materialize_smem_bytes(uint32_t W, uint32_t NP);
 void launch_init(const LevelParams& p, cudaStream_t s);
-void launch_level(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s);
+// Launches the level kernel of direction `dir` (DIR_PUSH / DIR_PULL), or
+// both (pull, then push) when dir is DIR_BOTH; `count` picks the form that
+// keeps the profiling counters.
+constexpr uint32_t DIR_BOTH = 2;
+void launch_level(const LevelParams& p, const LevelKernelInfo& k, uint32_t dir, bool count,
+                  cudaStream_t s);
 // reduce: per-source reductions (reduce_kernel) instead of rows or bitmasks.
 void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
                         cudaStream_t s);

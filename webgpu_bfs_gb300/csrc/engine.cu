@@ -74,6 +74,7 @@ struct Workspace {
   uint64_t graph_id = 0;
   uint32_t W = 0;
   uint32_t mode = 0;
+  bool count = false;  // level kernels keep the profiling counters
   LevelParams p{};
   LevelKernelInfo k{};
   LevelCtl* d_ctl = nullptr;
@@ -160,7 +161,7 @@ struct msbfs_engine {
   std::vector<msbfs_level_record> log;       // records of the last call
   LevelRec* h_log = nullptr;                 // pinned, LOG_CAP per pass
   size_t h_log_passes = 0;
-  std::vector<cudaEvent_t> lvl_events;       // profiling level 2
+  std::vector<cudaEvent_t> lvl_events;       // profiling levels 2 and 3
   std::vector<std::vector<float>> pass_event_ms;
   std::map<std::tuple<uint64_t, uint32_t, uint32_t>, std::unique_ptr<Workspace>> ws;
   // call scratch
@@ -292,14 +293,23 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w, bool reduce) {
   CK(cudaGraphAddNode(&n_cond, g, &n_init, nullptr, 1, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
 
+  // Loop body: the bottom-up kernel, then the top-down kernel; the one whose
+  // direction the control block does not name returns at once (a mode
+  // that never changes direction gets only its own).
   void* args_l[] = {&w->p, &h};
-  cudaKernelNodeParams kl{};
-  kl.func = w->k.level;
-  kl.gridDim = dim3(w->k.level_grid);
-  kl.blockDim = dim3(w->k.level_block);
-  kl.sharedMemBytes = 0;
-  kl.kernelParams = args_l;
-  CK(cudaGraphAddKernelNode(&n_lvl, body, nullptr, 0, &kl));
+  n_lvl = nullptr;
+  for (uint32_t dir : {(uint32_t)DIR_PULL, (uint32_t)DIR_PUSH}) {
+    if ((dir == DIR_PULL && w->mode == MODE_PUSH) || (dir == DIR_PUSH && w->mode == MODE_PULL))
+      continue;
+    cudaKernelNodeParams kl{};
+    kl.func = w->k.level[dir][w->count];
+    kl.gridDim = dim3(w->k.level_grids[dir]);
+    kl.blockDim = dim3(w->k.level_block);
+    kl.sharedMemBytes = 0;
+    kl.kernelParams = args_l;
+    cudaGraphNode_t prev = n_lvl;
+    CK(cudaGraphAddKernelNode(&n_lvl, body, prev ? &prev : nullptr, prev ? 1 : 0, &kl));
+  }
 
   cudaKernelNodeParams km{};
   km.func = reduce ? w->k.reduce : w->k.materialize;
@@ -347,7 +357,9 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   if (!level_kernel_info(W, NP, eng->num_sms, &w->k))
     return set_err(eng, MSBFS_ERR_INVALID_ARGUMENT, "unsupported words per vertex");
   // Work is claimed dynamically, so a smaller grid is only slower, never wrong.
-  w->k.level_grid = std::max(1, (int)((uint64_t)w->k.level_grid * eng->sm_share / 100));
+  w->count = eng->profiling == 1 || eng->profiling == 2;
+  for (int d = 0; d < 2; ++d)
+    w->k.level_grids[d] = std::max(1, (int)((uint64_t)w->k.level_grids[d] * eng->sm_share / 100));
   w->k.mat_grid = std::max(1, (int)((uint64_t)w->k.mat_grid * eng->sm_share / 100));
   w->k.red_grid = std::max(1, (int)((uint64_t)w->k.red_grid * eng->sm_share / 100));
   LevelParams& p = w->p;
@@ -452,11 +464,13 @@ int run_pass_profiled(msbfs_engine* eng, Workspace* w, bool reduce, std::vector<
     CK(cudaMemsetAsync(w->p.hlive, 0xFF, w->p.hlive_words * sizeof(uint32_t), eng->stream));
   launch_init(w->p, eng->stream);
   LevelCtl probe{};
+  CK(cudaMemcpyAsync(&probe, w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost, eng->stream));
+  CK(cudaStreamSynchronize(eng->stream));
   ms->clear();
   for (uint32_t L = 0;; ++L) {
     if ((rc = ensure_events(eng, 2))) return rc;
     CK(cudaEventRecord(eng->lvl_events[0], eng->stream));
-    launch_level(w->p, w->k, eng->stream);
+    launch_level(w->p, w->k, probe.dir, w->count, eng->stream);
     CK(cudaEventRecord(eng->lvl_events[1], eng->stream));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&probe, w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost, eng->stream));
@@ -491,7 +505,9 @@ int run_pass_host_loop(msbfs_engine* eng, Workspace* w, bool reduce) {
   launch_init(w->p, eng->stream);
   LevelCtl probe{};
   for (uint64_t launched = 0;;) {
-    for (int i = 0; i < 8; ++i) launch_level(w->p, w->k, eng->stream);
+    const uint32_t dirs = w->mode == MODE_PUSH ? DIR_PUSH : w->mode == MODE_PULL ? DIR_PULL
+                                                                                  : DIR_BOTH;
+    for (int i = 0; i < 8; ++i) launch_level(w->p, w->k, dirs, w->count, eng->stream);
     launched += 8;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&probe, w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost, eng->stream));
@@ -1037,8 +1053,15 @@ int msbfs_engine_set_level_cap(msbfs_engine* e, uint32_t max_levels) {
 }
 
 int msbfs_engine_set_profiling(msbfs_engine* e, int level) {
-  if (!e || level < 0 || level > 2) return MSBFS_ERR_INVALID_ARGUMENT;
+  if (!e || level < 0 || level > 3) return MSBFS_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(e->mu);
+  auto counting = [](int l) { return l == 1 || l == 2; };
+  if (counting(e->profiling) != counting(level)) {
+    // The captured graphs hold the counting or the production level kernels.
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    e->ws.clear();
+  }
   e->profiling = level;
   return MSBFS_OK;
 }

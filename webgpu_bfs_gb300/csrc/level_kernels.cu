@@ -2,8 +2,8 @@
 //
 // One pass traverses up to 32*W sources at once: lane s of word s/32 of a
 // vertex's W-word row belongs to source s. A level is one launch of
-// level_kernel<W>, which runs either a bottom-up (pull) or a top-down (push)
-// step, as decided on the device by the previous level; the loop itself is a
+// level_kernel<W, DIR>, a bottom-up (pull) or a top-down (push) step, as
+// decided on the device by the previous level; the loop itself is a
 // CUDA-graph WHILE node whose condition the last block of each level sets.
 //
 // Semantics follow the reference's WGSL kernels:
@@ -282,35 +282,43 @@ __device__ __forceinline__ uint32_t lane_word_mask(uint32_t P, uint32_t k) {
 }
 
 // Lane bits of the words [k0, k0+VEC) that are still worth discovering at
-// level L: sources of this pass whose frontier is non-empty.
+// level L (sources of this pass whose frontier is non-empty), from the
+// block's shared copy (kept out of registers: the gather loops need them).
 template <int VEC>
-__device__ __forceinline__ Words<VEC> alive_lanes(const LevelParams& p, uint32_t L, uint32_t k0) {
+__device__ __forceinline__ Words<VEC> alive_lanes(const uint32_t* s_alive, uint32_t k0) {
   Words<VEC> m;
-  const uint32_t P = p.desc->num_sources;
-  const volatile uint32_t* lanes = p.ctl->lanes[L & 1];
 #pragma unroll
-  for (int j = 0; j < VEC; ++j) m.w[j] = lane_word_mask(P, k0 + j) & lanes[k0 + j];
+  for (int j = 0; j < VEC; ++j) m.w[j] = s_alive[k0 + j];
   return m;
 }
 
 // Visited/frontier/level/queue writes for a vertex owned by the calling group
 // (all LPV lanes call it with their own VEC words).
+// The visited words are read again here rather than held in registers
+// through the gather loop (the group owns the vertex: nothing else writes
+// them during the level).
 template <int W, int VEC>
 __device__ __forceinline__ void pull_commit(const LevelParams& p, BlockQueue& bq, uint32_t* s_lanes,
                                             uint32_t L, uint32_t v, uint32_t k0, uint32_t lig,
-                                            const Words<VEC>& visw, const Words<VEC>& newly,
-                                            LevelCounters& cnt) {
-  Words<VEC> nv;
+                                            const Words<VEC>& newly, LevelCounters& cnt) {
 #pragma unroll
   for (int q = 0; q < VEC; ++q) {
-    nv.w[q] = visw.w[q] | newly.w[q];
     cnt.pairs += __popc(newly.w[q]);
     if (newly.w[q]) atomicOr(s_lanes + k0 + q, newly.w[q]);
   }
-  uint32_t* Fout = p.F[(L + 1) % 3];
-  st_words<VEC>(p.vis + (size_t)v * W + k0, nv);
-  st_words<VEC>(Fout + (size_t)v * W + k0, newly);
-  record_level<VEC, false>(p, v, k0, newly, L + 1);
+  // A lane whose words gained nothing leaves them as they are: its visited
+  // words are unchanged, its frontier words of level L+1 are already zero
+  // (cleared at level L-1) and its level-plane words need no bit. Late
+  // levels discover a lane or two per vertex, so most pieces skip.
+  if (any_bits<VEC>(newly)) {
+    uint32_t* Fout = p.F[(L + 1) % 3];
+    Words<VEC> nv = ld_words<VEC>(p.vis + (size_t)v * W + k0);
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) nv.w[q] |= newly.w[q];
+    st_words<VEC>(p.vis + (size_t)v * W + k0, nv);
+    st_words<VEC>(Fout + (size_t)v * W + k0, newly);
+    record_level<VEC, false>(p, v, k0, newly, L + 1);
+  }
   if (lig == 0) {
     cnt.newv += 1;
     atomicOr(p.fbits[(L + 1) % 3] + (v >> 5), 1u << (v & 31));
@@ -352,8 +360,8 @@ __device__ __forceinline__ uint32_t gather_id(const uint32_t* fb, uint32_t u) {
 //     words cover every lane still to be discovered. Vertices with in-degree
 //     >= heavy are scanned by the whole warp.
 template <int W>
-__device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lanes, uint32_t L,
-                           LevelCounters& cnt) {
+__device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lanes,
+                           const uint32_t* s_alive, uint32_t L, LevelCounters& cnt) {
   using G = Geo<W>;
   constexpr int VEC = G::VEC, LPV = G::LPV, GPW = G::GPW;
   const uint32_t lane = threadIdx.x & 31;
@@ -362,7 +370,6 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
   const uint32_t gid = lane / LPV;
   const uint32_t gmask = (LPV == 32) ? FULL : (((1u << LPV) - 1u) << gbase);
   const uint32_t k0 = lig * VEC;
-  const Words<VEC> lmask = alive_lanes<VEC>(p, L, k0);
   const uint32_t* __restrict__ Fin = p.F[L % 3];
   const uint32_t* __restrict__ fb =
       *(volatile uint32_t*)&p.ctl->use_bits ? p.fbits[L % 3] : nullptr;
@@ -392,6 +399,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     bool sat = true;
     uint32_t* hrow = p.hcand + (size_t)hk.h * W + k0;
     shared_c = ldcg_words<VEC>(hrow);
+    const Words<VEC> lmask = alive_lanes<VEC>(s_alive, k0);
 #pragma unroll
     for (int q = 0; q < VEC; ++q) {
       needed.w[q] = ~visw.w[q] & lmask.w[q];
@@ -475,7 +483,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         }
         st_words<VEC>(hrow, zero);
         const bool any_new = (__ballot_sync(gmask, any_bits<VEC>(newly)) & gmask) != 0;
-        if (any_new) pull_commit<W, VEC>(p, bq, s_lanes, L, v, k0, lig, visw, newly, cnt);
+        if (any_new) pull_commit<W, VEC>(p, bq, s_lanes, L, v, k0, lig, newly, cnt);
         if (lane == 0) p.hcount[hk.h] = 0;
       }
     }
@@ -518,11 +526,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
       beg = ent.y;
       end = ent.z;
     }
-    Words<VEC> needed, visw, cand;
+    Words<VEC> needed, cand;
 #pragma unroll
-    for (int j = 0; j < VEC; ++j) needed.w[j] = visw.w[j] = cand.w[j] = 0;
+    for (int j = 0; j < VEC; ++j) needed.w[j] = cand.w[j] = 0;
     if (end > beg) {
-      visw = ld_words<VEC>(p.vis + (size_t)v * W + k0);
+      const Words<VEC> visw = ld_words<VEC>(p.vis + (size_t)v * W + k0);
+      const Words<VEC> lmask = alive_lanes<VEC>(s_alive, k0);
 #pragma unroll
       for (int j = 0; j < VEC; ++j) needed.w[j] = ~visw.w[j] & lmask.w[j];
     }
@@ -646,7 +655,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
 #pragma unroll
     for (int q = 0; q < VEC; ++q) newly.w[q] = cand.w[q] & needed.w[q];
     const bool any_new = (__ballot_sync(FULL, any_bits<VEC>(newly)) & gmask) != 0;
-    if (any_new) pull_commit<W, VEC>(p, bq, s_lanes, L, v, k0, lig, visw, newly, cnt);
+    if (any_new) pull_commit<W, VEC>(p, bq, s_lanes, L, v, k0, lig, newly, cnt);
   }
 }
 
@@ -809,20 +818,39 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
   if (h) cudaGraphSetConditional(h, 1);
 }
 
-template <int W>
-__global__ void __launch_bounds__(LEVEL_BLOCK, MSBFS_LEVEL_MIN_BLOCKS)
+// One level of the traversal, bottom-up (DIR_PULL) or top-down (DIR_PUSH):
+// the two directions are separate kernels, each with its own register
+// budget, and both sit in the level loop's body -- the pull kernel first --
+// so the one whose direction the control block does not name returns at
+// once. When a pull level's controller turns the traversal top-down, the
+// push kernel of the same body iteration runs the next level. COUNT keeps
+// the per-level work counters of the profiling log (the production form
+// compiles them out; the discovered-pair count is always kept).
+#ifndef MSBFS_PUSH_MIN_BLOCKS
+#define MSBFS_PUSH_MIN_BLOCKS MSBFS_LEVEL_MIN_BLOCKS
+#endif
+template <int W, uint32_t DIR, bool COUNT>
+__global__ void __launch_bounds__(LEVEL_BLOCK, DIR == DIR_PULL ? MSBFS_LEVEL_MIN_BLOCKS
+                                                               : MSBFS_PUSH_MIN_BLOCKS)
     level_kernel(LevelParams p, cudaGraphConditionalHandle h) {
   __shared__ BlockQueue bq;
   __shared__ unsigned long long s_red[5][LEVEL_BLOCK / 32];
   __shared__ uint32_t s_lanes[W];
+  __shared__ uint32_t s_alive[W];
   __shared__ uint32_t s_last;
   volatile LevelCtl* c = p.ctl;
-  if (c->terminated) return;  // speculative launches of the host-driven loop
+  // Speculative launches of the host-driven loop, and the kernel of the
+  // other direction in the loop body, return here.
+  if (c->terminated || c->dir != DIR) return;
   const uint32_t L = c->level;
-  const uint32_t dir = c->dir;
   if (threadIdx.x == 0) {
     bq.count = 0;
     atomicMin(&p.ctl->t_start, globaltimer());
+  }
+  if constexpr (DIR == DIR_PULL) {
+    const uint32_t P = p.desc->num_sources;
+    for (uint32_t k = threadIdx.x; k < W; k += blockDim.x)
+      s_alive[k] = lane_word_mask(P, k) & c->lanes[L & 1][k];
   }
   for (uint32_t k = threadIdx.x; k < W; k += blockDim.x) s_lanes[k] = 0;
   __syncthreads();
@@ -846,8 +874,8 @@ __global__ void __launch_bounds__(LEVEL_BLOCK, MSBFS_LEVEL_MIN_BLOCKS)
   }
 
   LevelCounters cnt;
-  if (dir == DIR_PULL)
-    pull_phase<W>(p, bq, s_lanes, L, cnt);
+  if constexpr (DIR == DIR_PULL)
+    pull_phase<W>(p, bq, s_lanes, s_alive, L, cnt);
   else
     push_phase<W>(p, bq, s_lanes, L, cnt);
   flush_block_queue(p, bq, (L + 1) % 3);  // starts with a block barrier
@@ -855,8 +883,10 @@ __global__ void __launch_bounds__(LEVEL_BLOCK, MSBFS_LEVEL_MIN_BLOCKS)
     if (s_lanes[k]) atomicOr(&p.ctl->lanes[(L + 1) & 1][k], s_lanes[k]);
 
   unsigned long long vals[5] = {cnt.active, cnt.edges, cnt.newv, cnt.pairs, cnt.rows};
+  if constexpr (!COUNT) vals[0] = vals[1] = vals[2] = vals[4] = 0;
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
+    if (!COUNT && i != 3) continue;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vals[i] += __shfl_xor_sync(FULL, vals[i], o);
     if ((threadIdx.x & 31) == 0) s_red[i][threadIdx.x >> 5] = vals[i];
@@ -864,8 +894,10 @@ __global__ void __launch_bounds__(LEVEL_BLOCK, MSBFS_LEVEL_MIN_BLOCKS)
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long tot[5] = {0, 0, 0, 0, 0};
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 5; ++i) {
+      if (!COUNT && i != 3) continue;
       for (int w = 0; w < LEVEL_BLOCK / 32; ++w) tot[i] += s_red[i][w];
+    }
     if (tot[0]) atomicAdd(&p.ctl->c_active, tot[0]);
     if (tot[1]) atomicAdd(&p.ctl->c_edges, tot[1]);
     if (tot[2]) atomicAdd(&p.ctl->c_newv, tot[2]);
@@ -879,7 +911,7 @@ __global__ void __launch_bounds__(LEVEL_BLOCK, MSBFS_LEVEL_MIN_BLOCKS)
     s_last = (prev == gridDim.x - 1);
     if (s_last) {
       __threadfence();
-      controller(p, h, L, dir);
+      controller(p, h, L, DIR);
     }
   }
 }
@@ -1289,15 +1321,24 @@ __global__ void traversed_edges_kernel(uint32_t V, const uint32_t* __restrict__ 
 template <int W>
 static void fill_info(int num_sms, uint32_t NP, LevelKernelInfo* k) {
   k->init = (void*)init_kernel<W>;
-  k->level = (void*)level_kernel<W>;
+  k->level[DIR_PUSH][0] = (void*)level_kernel<W, DIR_PUSH, false>;
+  k->level[DIR_PUSH][1] = (void*)level_kernel<W, DIR_PUSH, true>;
+  k->level[DIR_PULL][0] = (void*)level_kernel<W, DIR_PULL, false>;
+  k->level[DIR_PULL][1] = (void*)level_kernel<W, DIR_PULL, true>;
   k->materialize = (void*)materialize_kernel<W>;
   k->reduce = (void*)reduce_kernel<W>;
   k->cleanup = (void*)cleanup_kernel<W>;
   k->level_block = LEVEL_BLOCK;
+  // The counting form runs at the production form's grid (it is only run
+  // for its counters; the roofline's durations come from the production form).
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, level_kernel<W>, LEVEL_BLOCK, 0);
-  if (occ < 1) occ = 1;
-  k->level_grid = num_sms * occ;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, level_kernel<W, DIR_PULL, false>,
+                                                LEVEL_BLOCK, 0);
+  k->level_grids[DIR_PULL] = num_sms * (occ < 1 ? 1 : occ);
+  occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, level_kernel<W, DIR_PUSH, false>,
+                                                LEVEL_BLOCK, 0);
+  k->level_grids[DIR_PUSH] = num_sms * (occ < 1 ? 1 : occ);
   k->mat_block = MAT_BLOCK;
   k->mat_smem = materialize_smem_bytes(W, NP);
   int mocc = 0;
@@ -1341,19 +1382,33 @@ void launch_init(const LevelParams& p, cudaStream_t s) {
   }
 }
 
-template <int W>
-static void launch_level_t(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
-  level_kernel<W><<<k.level_grid, k.level_block, 0, s>>>(p, (cudaGraphConditionalHandle)0);
+template <int W, bool COUNT>
+static void launch_level_t(const LevelParams& p, const LevelKernelInfo& k, uint32_t dir,
+                           cudaStream_t s) {
+  const cudaGraphConditionalHandle none = 0;
+  if (dir != DIR_PUSH)
+    level_kernel<W, DIR_PULL, COUNT><<<k.level_grids[DIR_PULL], k.level_block, 0, s>>>(p, none);
+  if (dir != DIR_PULL)
+    level_kernel<W, DIR_PUSH, COUNT><<<k.level_grids[DIR_PUSH], k.level_block, 0, s>>>(p, none);
 }
-void launch_level(const LevelParams& p, const LevelKernelInfo& k, cudaStream_t s) {
+template <int W>
+static void launch_level_w(const LevelParams& p, const LevelKernelInfo& k, uint32_t dir,
+                           bool count, cudaStream_t s) {
+  if (count)
+    launch_level_t<W, true>(p, k, dir, s);
+  else
+    launch_level_t<W, false>(p, k, dir, s);
+}
+void launch_level(const LevelParams& p, const LevelKernelInfo& k, uint32_t dir, bool count,
+                  cudaStream_t s) {
   switch (p.W) {
-    case 1: launch_level_t<1>(p, k, s); break;
-    case 2: launch_level_t<2>(p, k, s); break;
-    case 4: launch_level_t<4>(p, k, s); break;
-    case 8: launch_level_t<8>(p, k, s); break;
-    case 16: launch_level_t<16>(p, k, s); break;
-    case 32: launch_level_t<32>(p, k, s); break;
-    case 64: launch_level_t<64>(p, k, s); break;
+    case 1: launch_level_w<1>(p, k, dir, count, s); break;
+    case 2: launch_level_w<2>(p, k, dir, count, s); break;
+    case 4: launch_level_w<4>(p, k, dir, count, s); break;
+    case 8: launch_level_w<8>(p, k, dir, count, s); break;
+    case 16: launch_level_w<16>(p, k, dir, count, s); break;
+    case 32: launch_level_w<32>(p, k, dir, count, s); break;
+    case 64: launch_level_w<64>(p, k, dir, count, s); break;
   }
 }
 
