@@ -23,7 +23,7 @@ namespace msbfs {
 
 enum : uint32_t { DIR_PUSH = 0, DIR_PULL = 1 };
 enum : uint32_t { MODE_PUSH = 1, MODE_PULL = 2, MODE_HYBRID = 3 };
-enum : uint32_t { STATUS_LEVEL_CAP = 1u, STATUS_BAD_SOURCE = 2u };
+enum : uint32_t { STATUS_LEVEL_CAP = 1u, STATUS_BAD_SOURCE = 2u, STATUS_CHECK = 4u };
 
 // Per-level record written by the level controller (counters feed the
 // algorithmic-bytes model of the roofline; t is %globaltimer ns).
@@ -57,7 +57,7 @@ struct LevelCtl {
   uint32_t done_blocks;          // last-block-done counter of the level kernel
   uint32_t push_levels;
   uint32_t pull_levels;
-  uint32_t pad;
+  uint32_t check_site;           // bounds-checked build: first failed check site
   unsigned long long c_active;   // counters of the running level
   unsigned long long c_edges;
   unsigned long long c_newv;
@@ -127,7 +127,8 @@ struct LevelParams {
   LevelRec* log;      // LOG_CAP records
   const PassDesc* desc;
   uint32_t NP;        // planes allocated
-  uint32_t qcap;
+  uint32_t qcap;      // entries per queue slot (slots 1, 2)
+  uint32_t qcap0;     // entries of slot 0 (the sources' queue uses shorter entries)
   uint32_t mode;      // MODE_*
   uint32_t alpha;     // push -> pull when m_f * alpha > unexplored edges
   uint32_t beta;      // pull -> push when n_f * beta < V

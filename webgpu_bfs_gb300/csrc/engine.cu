@@ -376,6 +376,7 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   // entries bound it; the sources' queue (slot 0 at level 0) uses seg0.
   p.qcap = (uint32_t)std::min<uint64_t>(g->V + g->E / eng->seg + 1, 0xFFFFFFFFull);
   const uint64_t qcap0 = std::min<uint64_t>(g->V + g->E / MSBFS_PUSH_SEG0 + 1, 0xFFFFFFFFull);
+  p.qcap0 = (uint32_t)qcap0;
   p.mode = mode;
   p.alpha = eng->alpha;
   p.beta = eng->beta;
@@ -726,9 +727,10 @@ int finish_call(msbfs_engine* eng, msbfs_stats* stats) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, eng->ev_start, eng->ev_stop);
   eng->last.gpu_ms = ms;
-  uint32_t status = 0;
+  uint32_t status = 0, check_site = 0;
   for (size_t i = 0; i < eng->last_passes; ++i) {
     const LevelCtl& c = eng->h_ctl[i];
+    if (!check_site) check_site = c.check_site;
     eng->last.levels = std::max(eng->last.levels, c.level + 1);
     eng->last.push_levels += c.push_levels;
     eng->last.pull_levels += c.pull_levels;
@@ -770,6 +772,9 @@ int finish_call(msbfs_engine* eng, msbfs_stats* stats) {
     }
   }
   if (stats) *stats = eng->last;
+  if (status & STATUS_CHECK)
+    return set_err(eng, MSBFS_ERR_CUDA,
+                   "bounds check failed at site " + std::to_string(check_site));
   if (status & STATUS_LEVEL_CAP) return set_err(eng, MSBFS_ERR_TIMEOUT, "level cap reached");
   if (status & STATUS_BAD_SOURCE) return set_err(eng, MSBFS_ERR_SOURCE_OOB, "source out of range");
   return MSBFS_OK;

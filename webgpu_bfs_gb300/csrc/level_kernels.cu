@@ -48,6 +48,33 @@ constexpr int MAT_BLOCK = 256;
 constexpr uint32_t FULL = 0xffffffffu;
 constexpr uint32_t DIST_MAX = 0xffffffffu;
 
+// Bounds-checked build (-DMSBFS_BOUNDS_CHECK, the sanitizer's stand-in): an
+// index outside its buffer, or a loop past its iteration limit, records the
+// check's site id and STATUS_CHECK in the control block and skips the access
+// (or leaves the loop) instead of faulting or running on; the host turns it
+// into MSBFS_ERR_CUDA naming the site. The default build compiles the
+// checks out.
+#ifdef MSBFS_BOUNDS_CHECK
+__device__ __noinline__ void check_fail(LevelCtl* c, uint32_t site) {
+  atomicOr(&c->status, STATUS_CHECK);
+  atomicCAS(&c->check_site, 0u, site);
+}
+#define BCHECK(ok, site) ((ok) ? true : (check_fail(p.ctl, (site)), false))
+#define LOOP_GUARD(g, limit, site)  \
+  if (++(g) > (limit)) {            \
+    check_fail(p.ctl, (site));      \
+    break;                          \
+  }
+#else
+#define BCHECK(ok, site) true
+#define LOOP_GUARD(g, limit, site)
+#endif
+// Check sites (reported by the host as "bounds check failed at site N").
+enum : uint32_t {
+  CK_TILE_LOOP = 1, CK_ORDER_ENTRY = 3, CK_GATHER_ID = 4, CK_SLICE = 5,
+  CK_PUSH_ENTRY = 6, CK_PUSH_TARGET = 7, CK_CLEAR_ENTRY = 8, CK_QUEUE_CAP = 9
+};
+
 template <int W>
 struct Geo {
   static constexpr int VEC = W >= 4 ? 4 : W;  // words per lane access
@@ -147,7 +174,8 @@ __device__ void enqueue_global(const LevelParams& p, uint32_t slot, uint32_t v, 
   atomicAdd(&p.ctl->qverts[slot], 1u);
   atomicAdd(&p.ctl->qedges[slot], (unsigned long long)deg);
   for (uint32_t i = 0; i < n; ++i)
-    p.Q[slot][base + i] = ((unsigned long long)i << 32) | v;
+    if (BCHECK(base + i < (slot == 0 ? p.qcap0 : p.qcap), CK_QUEUE_CAP))
+      p.Q[slot][base + i] = ((unsigned long long)i << 32) | v;
 }
 
 __device__ __forceinline__ void bq_push(const LevelParams& p, BlockQueue& bq, uint32_t slot,
@@ -208,7 +236,9 @@ __device__ void flush_block_queue(const LevelParams& p, BlockQueue& bq, uint32_t
     const uint32_t v = bq.items[i];
     const uint32_t deg = p.out_off[v + 1] - p.out_off[v];
     const uint32_t ns = nseg_of(deg, p.seg);
-    for (uint32_t s = 0; s < ns; ++s) Q[pos++] = ((unsigned long long)s << 32) | v;
+    for (uint32_t s = 0; s < ns; ++s, ++pos)
+      if (BCHECK(pos < (slot == 0 ? p.qcap0 : p.qcap), CK_QUEUE_CAP))
+        Q[pos] = ((unsigned long long)s << 32) | v;
   }
 }
 
@@ -345,7 +375,9 @@ constexpr uint32_t TILE_BATCH = MSBFS_TILE_BATCH;
 // In-neighbour id as gathered: FULL when absent or, with a frontier bitmap,
 // outside the frontier (so its row is not loaded). The lane holding an id
 // tests it once for its whole group before the id is shuffled out.
-__device__ __forceinline__ uint32_t gather_id(const uint32_t* fb, uint32_t u) {
+__device__ __forceinline__ uint32_t gather_id(const LevelParams& p, const uint32_t* fb,
+                                              uint32_t u) {
+  if (u != FULL && !BCHECK(u < p.V, CK_GATHER_ID)) return FULL;
   return (u != FULL && in_frontier(fb, u)) ? u : FULL;
 }
 
@@ -391,6 +423,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     todo &= todo - 1;
     const HeavyChunk hk = p.hchunks[ci];
     const uint32_t v = hk.v;
+    if (!BCHECK(v < p.V && hk.j < hk.nch, CK_SLICE)) continue;
     const uint32_t vb = __ldg(in_off + v);
     const uint32_t beg = vb + hk.j * p.split;
     const uint32_t end = min(__ldg(in_off + v + 1), beg + p.split);
@@ -429,12 +462,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         if (lig == 0 && e0 < end) cnt.edges += min((uint32_t)CH, end - e0);
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
-          const uint32_t mine = gather_id(fb, ids[0]);
+          const uint32_t mine = gather_id(p, fb, ids[0]);
 #pragma unroll
           for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, mine, gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = gather_id(fb, ids[j]);
+          for (int j = 0; j < CH; ++j) u[j] = gather_id(p, fb, ids[j]);
         }
 #pragma unroll
         for (int j = 0; j < NI; ++j) {
@@ -499,7 +532,9 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
   const uint32_t per_stripe = (ntiles + WORK_STRIPES - 1) / WORK_STRIPES;
   uint32_t stripe = warp_g % WORK_STRIPES, exhausted = 0;
   uint32_t tile = 0, tile_end = 0;
+  [[maybe_unused]] uint32_t guard = 0;
   for (;;) {
+    LOOP_GUARD(guard, ntiles + 2 * WORK_STRIPES + 2, CK_TILE_LOOP)
     if (tile == tile_end) {
       // Claim from the warp's stripe; move to the next once it runs dry.
       while (exhausted < WORK_STRIPES) {
@@ -522,9 +557,11 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     uint32_t v = 0, beg = 0, end = 0;
     if (oi < p.n_order) {
       const uint4 ent = __ldg(p.order + oi);
-      v = ent.x;
-      beg = ent.y;
-      end = ent.z;
+      if (BCHECK(ent.x < p.V && ent.y <= ent.z && ent.z <= p.E, CK_ORDER_ENTRY)) {
+        v = ent.x;
+        beg = ent.y;
+        end = ent.z;
+      }
     }
     Words<VEC> needed, cand;
 #pragma unroll
@@ -553,12 +590,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
       for (uint32_t e0 = beg; e0 < end; e0 += CH) {
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
-          const uint32_t mine = gather_id(fb, ids[0]);
+          const uint32_t mine = gather_id(p, fb, ids[0]);
 #pragma unroll
           for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(gmask, mine, gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = gather_id(fb, ids[j]);
+          for (int j = 0; j < CH; ++j) u[j] = gather_id(p, fb, ids[j]);
         }
 #pragma unroll
         for (int j = 0; j < NI; ++j) {
@@ -616,12 +653,12 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         if (lig == 0 && e0 < hend) cnt.edges += min((uint32_t)CH, hend - e0);
         uint32_t u[CH];
         if constexpr (LPV >= CH) {
-          const uint32_t mine = gather_id(fb, ids[0]);
+          const uint32_t mine = gather_id(p, fb, ids[0]);
 #pragma unroll
           for (int j = 0; j < CH; ++j) u[j] = __shfl_sync(FULL, mine, gbase + j);
         } else {
 #pragma unroll
-          for (int j = 0; j < CH; ++j) u[j] = gather_id(fb, ids[j]);
+          for (int j = 0; j < CH; ++j) u[j] = gather_id(p, fb, ids[j]);
         }
 #pragma unroll
         for (int j = 0; j < NI; ++j) {
@@ -690,6 +727,7 @@ __device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     const unsigned long long ent = Qi[i];
     const uint32_t u = (uint32_t)ent;
     const uint32_t sg = (uint32_t)(ent >> 32);
+    if (!BCHECK(u < p.V, CK_PUSH_ENTRY)) continue;
     const Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u * W + k0);
     const uint32_t ob = __ldg(p.out_off + u), oe = __ldg(p.out_off + u + 1);
     const uint32_t eb = ob + sg * seg;
@@ -699,6 +737,7 @@ __device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
     // edge is processed. A stale visited word only widens `needed`; the
     // atomicOr's previous value decides what is new.
     uint32_t vn = eb < ee ? __ldg(p.out_idx + eb) : 0u;
+    if (!BCHECK(vn < p.V, CK_PUSH_TARGET)) vn = 0;
     Words<VEC> vwn;
     if (eb < ee) vwn = ldcg_words<VEC>(p.vis + (size_t)vn * W + k0);
     for (uint32_t e = eb; e < ee; ++e) {
@@ -707,6 +746,7 @@ __device__ void push_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
       const Words<VEC> vw = vwn;
       if (e + 1 < ee) {
         vn = __ldg(p.out_idx + e + 1);
+        if (!BCHECK(vn < p.V, CK_PUSH_TARGET)) vn = 0;
         vwn = ldcg_words<VEC>(p.vis + (size_t)vn * W + k0);
       }
       bool found = false;
@@ -818,6 +858,21 @@ __device__ void controller(const LevelParams& p, cudaGraphConditionalHandle h, u
   if (h) cudaGraphSetConditional(h, 1);
 }
 
+// Zeroes the frontier words of the n entries of queue slot `sl` (entries
+// with a non-zero segment repeat a vertex, so only segment 0 clears).
+template <int W>
+__device__ __forceinline__ void clear_frontier_rows(const LevelParams& p, uint32_t sl, uint32_t n,
+                                                    size_t t0, size_t nthreads) {
+  const unsigned long long* Q = p.Q[sl];
+  uint32_t* F = p.F[sl];
+  const size_t total = (size_t)n * W;
+  for (size_t i = t0; i < total; i += nthreads) {
+    const unsigned long long ent = Q[i / W];
+    if ((ent >> 32) == 0 && BCHECK((uint32_t)ent < p.V, CK_CLEAR_ENTRY))
+      F[(size_t)(uint32_t)ent * W + i % W] = 0;
+  }
+}
+
 // One level of the traversal, bottom-up (DIR_PULL) or top-down (DIR_PUSH):
 // the two directions are separate kernels, each with its own register
 // budget, and both sit in the level loop's body -- the pull kernel first --
@@ -858,15 +913,8 @@ __global__ void __launch_bounds__(LEVEL_BLOCK, DIR == DIR_PULL ? MSBFS_LEVEL_MIN
   // Clear the frontier words of level L-1 (not read or written this level).
   {
     const uint32_t sc = (L + 2) % 3;
-    const uint32_t n = c->qcount[sc];
-    const unsigned long long* Qc = p.Q[sc];
-    uint32_t* Fc = p.F[sc];
-    const size_t total = (size_t)n * W;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-         i += (size_t)gridDim.x * blockDim.x) {
-      const unsigned long long ent = Qc[i / W];
-      if ((ent >> 32) == 0) Fc[(size_t)(uint32_t)ent * W + i % W] = 0;
-    }
+    clear_frontier_rows<W>(p, sc, c->qcount[sc], blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                           (size_t)gridDim.x * blockDim.x);
     uint32_t* fc = p.fbits[sc];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (p.V + 31) / 32;
          i += gridDim.x * blockDim.x)
@@ -1284,18 +1332,10 @@ size_t materialize_smem_bytes(uint32_t W, uint32_t NP) {
 template <int W>
 __global__ void cleanup_kernel(LevelParams p) {
   const uint32_t L = p.ctl->level;
-  for (uint32_t k = 0; k < 2; ++k) {
-    const uint32_t sl = (L + k) % 3;
-    const uint32_t n = p.ctl->qcount[sl];
-    const unsigned long long* Qs = p.Q[sl];
-    uint32_t* Fs = p.F[sl];
-    const size_t total = (size_t)n * W;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-         i += (size_t)gridDim.x * blockDim.x) {
-      const unsigned long long ent = Qs[i / W];
-      if ((ent >> 32) == 0) Fs[(size_t)(uint32_t)ent * W + i % W] = 0;
-    }
-  }
+  for (uint32_t k = 0; k < 2; ++k)
+    clear_frontier_rows<W>(p, (L + k) % 3, p.ctl->qcount[(L + k) % 3],
+                           blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                           (size_t)gridDim.x * blockDim.x);
 }
 
 // Traversed edges of a distance matrix (crates/cli/src/bench.rs:478-491).
