@@ -151,6 +151,40 @@ int msbfs_engine_set_stream(msbfs_engine *engine, void *cuda_stream);
  * chunks in multi_word_bp.rs:630). Zero keeps the current value. */
 int msbfs_engine_set_tuning(msbfs_engine *engine, uint32_t max_words_per_pass,
                             uint32_t alpha, uint32_t beta);
+/* Autotuner of the level-synchronous path. No single reference
+ * counterpart: the reference fixes its thresholds -- alpha = 14 / beta = 24
+ * for the direction switch (crates/gpu_bfs/src/dispatch/push_pull.rs:29-36),
+ * the bottom-up density threshold of the hybrid prep kernel
+ * (crates/shaders/src/prep_hybrid_hop.wgsl:67-71) and 512-source chunks
+ * (crates/gpu_bfs/src/dispatch/multi_word_bp.rs:630) -- and picks a method
+ * per call by fixed rules (engine.rs:157-198). For the graph's class
+ * (road-like / mesh / power-law x vertex-count bucket, the batched form's
+ * classes) and the source count rounded up to a power of two, the autotuner
+ * times the call on the given sources (per-source statistics output, CUDA
+ * events) while it varies one setting at a time over its candidates -- words
+ * per vertex of a pass, alpha, beta, the in-edge slice length of bottom-up
+ * steps and the frontier-bitmap threshold -- keeping a change only when it is
+ * faster, then applies the best settings to the engine (and the slice length
+ * to the graph). With a cache path, a class already in the file is applied
+ * without timing and new classes are appended. Results never depend on the
+ * settings. Calls that the router sends to the CTA-per-source path are not
+ * tuned (the settings do not apply to it). */
+typedef struct msbfs_tuning {
+  uint32_t max_words_per_pass; /* u32 words per vertex of a pass (32 sources each) */
+  uint32_t alpha;              /* top-down -> bottom-up: frontier out-edges * alpha > E */
+  uint32_t beta;               /* bottom-up -> top-down: frontier vertices * beta < V  */
+  uint32_t hub_split;          /* in-edge slice length of bottom-up steps              */
+  uint32_t bitmap_div;         /* frontier-bitmap test below V / bitmap_div vertices    */
+  uint32_t from_cache;         /* 1: read from the cache file, not timed               */
+  uint32_t trials;             /* settings timed                                        */
+  uint32_t level_path;         /* 0: the call runs on the CTA path, nothing tuned       */
+  double ms;                   /* device time of one call with the chosen settings     */
+  double default_ms;           /* the same with the settings the engine had before     */
+  char class_name[48];         /* graph class and source bucket, "powerlaw/v2^22/s512" */
+} msbfs_tuning;
+int msbfs_engine_autotune(msbfs_engine *engine, msbfs_graph *graph, const uint32_t *sources,
+                          size_t num_sources, const char *cache_path, msbfs_tuning *out);
+
 /* Caps the persistent kernels' grids at `percent` (1..100, default 100) of
  * the blocks that fit the device at once, leaving the rest of the SMs to
  * kernels of other streams (the served form gives them to its express

@@ -44,6 +44,11 @@ STRUCTS = {
     "msbfs_mtx_error": ("MtxErrorInfo", [
         ("kind", "kind"), ("line_number", "line_number"), ("row", "row"), ("col", "col"),
         ("max_rows", "max_rows"), ("max_cols", "max_cols"), ("message", "message")]),
+    "msbfs_tuning": ("Tuning", [
+        ("max_words_per_pass", "max_words_per_pass"), ("alpha", "alpha"), ("beta", "beta"),
+        ("hub_split", "hub_split"), ("bitmap_div", "bitmap_div"), ("from_cache", "from_cache"),
+        ("trials", "trials"), ("level_path", "level_path"), ("ms", "ms"),
+        ("default_ms", "default_ms"), ("class_name", "class_name")]),
     "msbfs_batch_graph": ("BatchGraph", [
         ("num_vertices", "num_vertices"), ("num_edges", "num_edges"),
         ("row_offsets", "row_offsets"), ("col_indices", "col_indices"),

@@ -332,3 +332,40 @@ def test_level_cap_times_out_and_engine_recovers(native, oracle, monkeypatch, lo
             assert_same(got, want, g, deep, f"{loop} loop after the cap, {method}")
     finally:
         eng.close()
+
+
+def test_autotune_same_bytes_and_cache(native, oracle, tmp_path):
+    """The level-path autotuner changes speed, never results: rows after
+    tuning equal the oracle's; the chosen settings are cached per graph
+    class and source bucket, and a fresh engine applies them from the file
+    without timing. A road-like graph's calls go to the CTA path and are
+    not tuned."""
+    cache = str(tmp_path / "level_tuning.txt")
+    g = native.generate_graph500_rmat(13, 16, 91)
+    src = native.sample_sources(g, 300, 4, min_degree=1)
+    want = _oracle(oracle, g, src)
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.Auto)
+    try:
+        t = eng.autotune(g, src, cache_path=cache)
+        assert t["level_path"] == 1 and not t["from_cache"] and t["trials"] >= 10
+        assert t["class_name"] == "powerlaw/v2^12/s512" and 0 < t["ms"] <= t["default_ms"]
+        assert t["max_words_per_pass"] in (4, 8, 16) and t["hub_split"] in (256, 512, 1024)
+        assert_same(eng.run_ms_bfs(g, src), want, g, src, f"tuned {t}")
+        other = native.sample_sources(g, 260, 5, min_degree=1)  # same bucket, other sources
+        assert_same(eng.run_ms_bfs(g, other), _oracle(oracle, g, other), g, other, "tuned, other")
+    finally:
+        eng.close()
+    eng = native.GpuBfsEngine(native.GpuBfsMethod.Auto)
+    try:
+        t2 = eng.autotune(g, src, cache_path=cache)
+        assert t2["from_cache"] and t2["trials"] == 0
+        assert {k: t2[k] for k in ("max_words_per_pass", "alpha", "beta", "hub_split",
+                                   "bitmap_div")} == \
+            {k: t[k] for k in ("max_words_per_pass", "alpha", "beta", "hub_split", "bitmap_div")}
+        assert_same(eng.run_ms_bfs(g, src), want, g, src, "settings from the cache")
+        road = native.wilson_grid(50, 50, 40, 2)
+        rs = native.sample_sources(road, 40, 1)
+        assert eng.autotune(road, rs)["level_path"] == 0
+        assert len(open(cache).read().splitlines()) == 1
+    finally:
+        eng.close()

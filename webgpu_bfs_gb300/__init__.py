@@ -403,6 +403,19 @@ class GpuBfsEngine:
         self._check(_native.lib().msbfs_engine_set_tuning(self._h, max_words_per_pass, alpha,
                                                           beta))
 
+    def autotune(self, graph: CsrGraph, sources, cache_path: Optional[str] = None) -> dict:
+        """Tunes the level path's settings for the graph's class and this
+        source count (msbfs_engine_autotune) and applies them; returns the
+        chosen settings, the tuned and default call times and the class."""
+        src = _u32(sources)
+        dg = self.upload(graph)
+        t = _native.Tuning()
+        rc = _native.lib().msbfs_engine_autotune(
+            self._h, dg.handle, _ptr(src), src.size,
+            cache_path.encode() if cache_path else None, C.byref(t))
+        self._check(rc)
+        return t.as_dict()
+
     def set_level_cap(self, max_levels: int) -> None:
         """Stops a level-synchronous pass after ``max_levels`` levels with
         BfsError code 4 (Timeout); 0 restores the default (V + 2)."""

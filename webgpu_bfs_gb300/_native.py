@@ -104,6 +104,27 @@ class MtxErrorInfo(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("max_words_per_pass", C.c_uint32),
+        ("alpha", C.c_uint32),
+        ("beta", C.c_uint32),
+        ("hub_split", C.c_uint32),
+        ("bitmap_div", C.c_uint32),
+        ("from_cache", C.c_uint32),
+        ("trials", C.c_uint32),
+        ("level_path", C.c_uint32),
+        ("ms", C.c_double),
+        ("default_ms", C.c_double),
+        ("class_name", C.c_char * 48),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["class_name"] = d["class_name"].decode()
+        return d
+
+
 # numpy view of msbfs_source_stats
 SOURCE_STATS_DTYPE = [("distance_sum", "<u8"), ("eccentricity", "<u4"), ("reached", "<u4")]
 
@@ -128,6 +149,8 @@ SIGNATURES = {
     "msbfs_engine_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "msbfs_engine_set_tuning": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]),
     "msbfs_engine_set_sm_share": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "msbfs_engine_autotune": (C.c_int, [C.c_void_p, C.c_void_p, u32p, C.c_size_t, C.c_char_p,
+                                        C.POINTER(Tuning)]),
     "msbfs_engine_set_level_cap": (C.c_int, [C.c_void_p, C.c_uint32]),
     "msbfs_engine_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "msbfs_engine_level_log": (C.c_int, [C.c_void_p, C.POINTER(LevelRecord), C.c_size_t,

@@ -277,12 +277,7 @@ struct HostGraphInfo {
 };
 
 std::string class_key(size_t V, size_t E, uint32_t max_deg) {
-  const char* kind = (max_deg <= 8 && E <= 4 * V) ? "road" : (max_deg >= 128 ? "powerlaw" : "mesh");
-  int lv = 0;
-  while ((size_t(1) << (lv + 1)) <= V) ++lv;
-  char buf[64];
-  snprintf(buf, sizeof buf, "%s/v2^%d", kind, lv / 2 * 2);
-  return buf;
+  return msbfs::graph_class(V, E, max_deg);
 }
 
 int cuda_err(cudaError_t e) {

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -66,6 +67,7 @@ struct msbfs_graph {
   uint4* order = nullptr;  // {vertex, in-edge begin, in-edge end, 0}
   // Road-like graphs: per edge {target, target's edge begin, end, 0}.
   uint4* erec = nullptr;
+  std::vector<uint32_t> h_coff;  // host CSC offsets (V + 1): rebuilds the tables above
 };
 
 namespace {
@@ -780,6 +782,75 @@ int finish_call(msbfs_engine* eng, msbfs_stats* stats) {
   return MSBFS_OK;
 }
 
+// Slice table of in-edge lists longer than `split` and the bottom-up work
+// list of the other vertices with in-edges, from the graph's host CSC
+// offsets. Rebuilt when the autotuner changes the slice length; the caller
+// drops the workspaces that point at the old tables first.
+int build_bottom_up_tables(msbfs_engine* eng, msbfs_graph* g, uint32_t split) {
+  const size_t V = g->V;
+  const std::vector<uint32_t>& coff = g->h_coff;
+  cudaFree(g->hchunks);
+  cudaFree(g->order);
+  g->hchunks = nullptr;
+  g->order = nullptr;
+  g->split = split;
+  g->n_heavy = 0;
+  std::vector<HeavyChunk> chunks;
+  for (size_t v = 0; v < V; ++v) {
+    const uint32_t indeg = coff[v + 1] - coff[v];
+    if (indeg <= split) continue;
+    const uint32_t nch = (indeg + split - 1) / split;
+    for (uint32_t j = 0; j < nch; ++j) chunks.push_back(HeavyChunk{(uint32_t)v, j, nch, g->n_heavy});
+    g->n_heavy++;
+  }
+  // Longest lists first so their slices start early in every bottom-up step.
+  std::stable_sort(chunks.begin(), chunks.end(), [](const HeavyChunk& a, const HeavyChunk& b) {
+    return a.nch > b.nch;
+  });
+  g->n_hchunks = (uint32_t)chunks.size();
+  CK(cudaMalloc((void**)&g->hchunks, std::max<size_t>(chunks.size(), 1) * sizeof(HeavyChunk)));
+  if (!chunks.empty())
+    CK(cudaMemcpy(g->hchunks, chunks.data(), chunks.size() * sizeof(HeavyChunk),
+                  cudaMemcpyHostToDevice));
+  // Bottom-up work list: the vertices with 0 < in-degree <= split, ascending
+  // ids (neighbouring vertices share cache lines of the visited and frontier
+  // rows). MSBFS_ORDER_WINDOW > 1 sorts by in-degree, descending, within
+  // windows of that many entries, so the groups of a warp scan in-edge lists
+  // of similar length; on R-MAT scale 22, S=512 the lost locality outweighs
+  // the balance (window 256: +8%, window 1024: +10% bottom-up time), so the
+  // default keeps plain id order.
+#ifndef MSBFS_ORDER_WINDOW
+#define MSBFS_ORDER_WINDOW 0
+#endif
+  std::vector<uint32_t> order;
+  order.reserve(V);
+  for (size_t v = 0; v < V; ++v) {
+    const uint32_t d = coff[v + 1] - coff[v];
+    if (d > 0 && d <= split) order.push_back((uint32_t)v);
+  }
+  const size_t win = MSBFS_ORDER_WINDOW;
+  if (win > 1) {
+    auto deg_desc = [&](uint32_t a, uint32_t b) {
+      return coff[a + 1] - coff[a] > coff[b + 1] - coff[b];
+    };
+    for (size_t i = 0; i < order.size(); i += win)
+      std::stable_sort(order.begin() + i, order.begin() + std::min(order.size(), i + win),
+                       deg_desc);
+  }
+  g->n_order = (uint32_t)order.size();
+  // Each entry carries the vertex and its in-edge range, so a bottom-up
+  // step starts a vertex's scan one dependent load earlier.
+  std::vector<uint4> ent(order.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    const uint32_t v = order[i];
+    ent[i] = make_uint4(v, coff[v], coff[v + 1], 0u);
+  }
+  CK(cudaMalloc((void**)&g->order, std::max<size_t>(ent.size(), 1) * sizeof(uint4)));
+  if (!ent.empty())
+    CK(cudaMemcpy(g->order, ent.data(), ent.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+  return MSBFS_OK;
+}
+
 int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, const uint32_t* idx,
                  msbfs_graph** out) {
   if (!eng || !out) return MSBFS_ERR_INVALID_ARGUMENT;
@@ -811,63 +882,9 @@ int upload_graph(msbfs_engine* eng, size_t V, size_t E, const uint32_t* off, con
     CK(cudaMemcpy(g->coff, t.off.data(), (V + 1) * 4, cudaMemcpyHostToDevice));
     if (E) CK(cudaMemcpy(g->cidx, t.idx.data(), E * 4, cudaMemcpyHostToDevice));
   }
-  // Slice table of long in-edge lists (in-degree = CSC row length).
-  g->split = eng->split;
-  std::vector<HeavyChunk> chunks;
-  for (size_t v = 0; v < V; ++v) {
-    const uint32_t indeg = t.off[v + 1] - t.off[v];
-    if (indeg <= g->split) continue;
-    const uint32_t nch = (indeg + g->split - 1) / g->split;
-    for (uint32_t j = 0; j < nch; ++j) chunks.push_back(HeavyChunk{(uint32_t)v, j, nch, g->n_heavy});
-    g->n_heavy++;
-  }
-  // Longest lists first so their slices start early in every bottom-up step.
-  std::stable_sort(chunks.begin(), chunks.end(), [](const HeavyChunk& a, const HeavyChunk& b) {
-    return a.nch > b.nch;
-  });
-  g->n_hchunks = (uint32_t)chunks.size();
-  CK(cudaMalloc((void**)&g->hchunks, std::max<size_t>(chunks.size(), 1) * sizeof(HeavyChunk)));
-  if (!chunks.empty())
-    CK(cudaMemcpy(g->hchunks, chunks.data(), chunks.size() * sizeof(HeavyChunk),
-                  cudaMemcpyHostToDevice));
-  // Bottom-up work list: the vertices with 0 < in-degree <= split, ascending
-  // ids (neighbouring vertices share cache lines of the visited and frontier
-  // rows). MSBFS_ORDER_WINDOW > 1 sorts by in-degree, descending, within
-  // windows of that many entries, so the groups of a warp scan in-edge lists
-  // of similar length; on R-MAT scale 22, S=512 the lost locality outweighs
-  // the balance (window 256: +8%, window 1024: +10% bottom-up time), so the
-  // default keeps plain id order.
-  {
-#ifndef MSBFS_ORDER_WINDOW
-#define MSBFS_ORDER_WINDOW 0
-#endif
-    std::vector<uint32_t> order;
-    order.reserve(V);
-    for (size_t v = 0; v < V; ++v) {
-      const uint32_t d = t.off[v + 1] - t.off[v];
-      if (d > 0 && d <= g->split) order.push_back((uint32_t)v);
-    }
-    const size_t win = MSBFS_ORDER_WINDOW;
-    if (win > 1) {
-      auto deg_desc = [&](uint32_t a, uint32_t b) {
-        return t.off[a + 1] - t.off[a] > t.off[b + 1] - t.off[b];
-      };
-      for (size_t i = 0; i < order.size(); i += win)
-        std::stable_sort(order.begin() + i, order.begin() + std::min(order.size(), i + win),
-                         deg_desc);
-    }
-    g->n_order = (uint32_t)order.size();
-    // Each entry carries the vertex and its in-edge range, so a bottom-up
-    // step starts a vertex's scan one dependent load earlier.
-    std::vector<uint4> ent(order.size());
-    for (size_t i = 0; i < order.size(); ++i) {
-      const uint32_t v = order[i];
-      ent[i] = make_uint4(v, t.off[v], t.off[v + 1], 0u);
-    }
-    CK(cudaMalloc((void**)&g->order, std::max<size_t>(ent.size(), 1) * sizeof(uint4)));
-    if (!ent.empty())
-      CK(cudaMemcpy(g->order, ent.data(), ent.size() * sizeof(uint4), cudaMemcpyHostToDevice));
-  }
+  g->h_coff = std::move(t.off);
+  int rc = build_bottom_up_tables(eng, g.get(), eng->split);
+  if (rc) return rc;
   // Road-like graphs (the ones the router sends to the CTA path) get edge
   // records, 16 bytes per edge, so a CTA-path level costs one dependent L2
   // round trip instead of three.
@@ -1271,3 +1288,140 @@ int msbfs_traversed_edges_device(msbfs_engine* e, const msbfs_graph* g, const ui
 }
 
 }  // extern "C"
+
+// ============================================================ level autotuner
+
+namespace {
+
+// Settings of the level-synchronous path that the autotuner varies.
+struct LevelSettings {
+  uint32_t words, alpha, beta, split, bits_div;
+  uint32_t& at(int i) {
+    return i == 0 ? words : i == 1 ? alpha : i == 2 ? beta : i == 3 ? split : bits_div;
+  }
+  bool operator==(const LevelSettings& o) const {
+    return words == o.words && alpha == o.alpha && beta == o.beta && split == o.split &&
+           bits_div == o.bits_div;
+  }
+};
+
+// The thresholds are baked into an engine's captured graphs, so its
+// workspaces are dropped; a new slice length rebuilds the graph's bottom-up
+// tables (done only when no other engine runs on the graph).
+int apply_settings(msbfs_engine* eng, msbfs_graph* g, const LevelSettings& s) {
+  CK(cudaStreamSynchronize(eng->stream));
+  CK(cudaStreamSynchronize(eng->copy_stream));
+  eng->ws.clear();
+  eng->max_words = s.words;
+  eng->alpha = s.alpha;
+  eng->beta = s.beta;
+  eng->bits_div = s.bits_div;
+  if (s.split != g->split) return build_bottom_up_tables(eng, g, s.split);
+  return MSBFS_OK;
+}
+
+// Device time (CUDA events) of one per-source-statistics call: the smaller
+// of two after a call that builds the workspace.
+int time_stats_call(msbfs_engine* eng, msbfs_graph* g, const uint32_t* src, size_t S, int method,
+                    double* ms) {
+  int rc;
+  if ((rc = grow(eng, &eng->d_sstats, &eng->d_sstats_cap, S))) return rc;
+  double best = 1e30;
+  for (int k = 0; k < 3; ++k) {
+    if ((rc = enqueue_call(eng, method, g, src, S, nullptr, nullptr, nullptr, nullptr,
+                           eng->d_sstats)))
+      return rc;
+    msbfs_stats st{};
+    if ((rc = finish_call(eng, &st))) return rc;
+    if (k > 0) best = std::min(best, st.gpu_ms);
+  }
+  *ms = best;
+  return MSBFS_OK;
+}
+
+}  // namespace
+
+extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint32_t* sources,
+                                     size_t S, const char* cache_path, msbfs_tuning* out) {
+  if (!e) return MSBFS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(e->mu);
+  msbfs_engine* eng = e;
+  int rc = validate_call(e, g, sources, S);
+  if (rc) return rc;
+  if (S == 0 || g->V == 0) return set_err(e, MSBFS_ERR_INVALID_ARGUMENT, "autotune needs sources");
+  CK(cudaSetDevice(e->device));
+  size_t bucket = 1;
+  while (bucket < S) bucket <<= 1;
+  const std::string key =
+      msbfs::graph_class(g->V, g->E, g->max_deg) + "/s" + std::to_string(bucket);
+  msbfs_tuning t{};
+  std::strncpy(t.class_name, key.c_str(), sizeof t.class_name - 1);
+  LevelSettings best{e->max_words, e->alpha, e->beta, g->split, e->bits_div};
+  auto report = [&](const LevelSettings& s) {
+    t.max_words_per_pass = s.words;
+    t.alpha = s.alpha;
+    t.beta = s.beta;
+    t.hub_split = s.split;
+    t.bitmap_div = s.bits_div;
+    if (out) *out = t;
+    return MSBFS_OK;
+  };
+  const int method = resolve_method(g, e->method, S);
+  if (method_path(method) == MSBFS_PATH_CTA) return report(best);
+  t.level_path = 1;
+  const bool shared = !g->users.empty() || g->eng != e;  // other engines hold its tables
+  // Cache: one line per class, "class words alpha beta split bitmap_div ms".
+  if (cache_path) {
+    std::ifstream in(cache_path);
+    std::string k;
+    LevelSettings s{};
+    double ms = 0;
+    while (in >> k >> s.words >> s.alpha >> s.beta >> s.split >> s.bits_div >> ms) {
+      if (k != key) continue;
+      if (shared) s.split = g->split;
+      if ((rc = apply_settings(e, g, s))) return rc;
+      t.from_cache = 1;
+      t.ms = ms;
+      return report(s);
+    }
+  }
+  double best_ms = 0;
+  if ((rc = time_stats_call(e, g, sources, S, method, &best_ms))) return rc;
+  t.default_ms = best_ms;
+  t.trials = 1;
+  uint32_t wmax = 1;
+  while (wmax < (S + 31) / 32 && wmax < 64) wmax <<= 1;
+  const std::vector<std::vector<uint32_t>> cands = {
+      {std::max(1u, wmax / 4), std::max(1u, wmax / 2), wmax},  // words per vertex
+      {4, 8, 14, 28, 56},                                      // alpha
+      {6, 12, 24, 64, 256},                                    // beta
+      {256, 512, 1024},                                        // slice length
+      {16, 64, 256}};                                          // bitmap divisor
+  // One setting at a time, each from the best found so far; a change is
+  // kept only when it is at least 2% faster (timing noise).
+  for (int i = 0; i < 5; ++i) {
+    if (i == 3 && shared) continue;
+    const LevelSettings base = best;
+    for (uint32_t c : cands[i]) {
+      LevelSettings s = base;
+      s.at(i) = c;
+      if (s == base) continue;
+      if ((rc = apply_settings(e, g, s))) return rc;
+      double ms = 0;
+      if ((rc = time_stats_call(e, g, sources, S, method, &ms))) return rc;
+      ++t.trials;
+      if (ms < best_ms * 0.98) {
+        best_ms = ms;
+        best = s;
+      }
+    }
+  }
+  if ((rc = apply_settings(e, g, best))) return rc;
+  t.ms = best_ms;
+  if (cache_path) {
+    std::ofstream o(cache_path, std::ios::app);
+    o << key << ' ' << best.words << ' ' << best.alpha << ' ' << best.beta << ' ' << best.split
+      << ' ' << best.bits_div << ' ' << best_ms << '\n';
+  }
+  return report(best);
+}

@@ -180,6 +180,13 @@ std::string validate(size_t V, size_t E, const uint32_t* off, const uint32_t* id
   return std::string();
 }
 
+std::string graph_class(size_t V, size_t E, uint32_t max_deg) {
+  const char* kind = (max_deg <= 8 && E <= 4 * V) ? "road" : (max_deg >= 128 ? "powerlaw" : "mesh");
+  int lv = 0;
+  while ((size_t(1) << (lv + 1)) <= V) ++lv;
+  return std::string(kind) + "/v2^" + std::to_string(lv / 2 * 2);
+}
+
 uint32_t max_degree(size_t V, const uint32_t* off) {
   uint32_t m = 0;
   for (size_t u = 0; u < V; ++u) m = std::max(m, off[u + 1] - off[u]);

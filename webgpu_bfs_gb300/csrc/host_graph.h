@@ -53,6 +53,12 @@ std::string validate(size_t V, size_t E, const uint32_t* off, const uint32_t* id
                      size_t idx_len);
 uint32_t max_degree(size_t V, const uint32_t* off);
 
+// Graph class of the autotuners (batched form and level path): road-like
+// (max degree <= 8, E <= 4V: the router's CTA-path test), power-law (max
+// degree >= 128) or mesh, and the vertex count rounded down to an even
+// power of two, e.g. "powerlaw/v2^22".
+std::string graph_class(size_t V, size_t E, uint32_t max_deg);
+
 // Generators (generators.rs), seeded with SplitMix64.
 HostCsr gen_grid2d(size_t w, size_t h);
 HostCsr gen_erdos_renyi_np(size_t n, double p, uint64_t seed);
