@@ -988,8 +988,10 @@ def run_served(args, spec):
 
 
 def run_ncu_case(args, spec):
-    """A single small invocation for ncu captures (few GB on the device)."""
-    os.environ["MSBFS_HOST_LOOP"] = "1"
+    """A single small invocation for ncu captures (few GB on the device). The
+    level loop is driven from the host one level at a time with the
+    production kernels (profiling level 3), so launch i of the level kernels
+    is level i."""
     import __graft_entry__
     __graft_entry__.build()
     import webgpu_bfs_gb300 as m
@@ -1015,6 +1017,7 @@ def run_ncu_case(args, spec):
     g = make_graph(m, spec)
     src = m.sample_sources(g, spec["S"], spec["seed"], min_degree=1)
     eng = m.GpuBfsEngine(m.GpuBfsMethod.Auto)
+    eng.set_profiling(3)
     if args.ncu_case == "level":
         eng.run_ms_reachability(g, src)
         print("ncu case ok", json.dumps(eng.last_stats))

@@ -297,10 +297,13 @@ int msbfs_run_ms_bfs_stats(msbfs_engine *engine, const msbfs_graph *graph,
  * unrelated requests share the source lanes of one traversal -- so requests
  * arriving while others run are admitted as slots free up and their work
  * overlaps on the device. Admission is by device bytes: each slot's
- * traversal state is allocated once, and distance rows are staged in at most
- * hbm_budget_bytes / slots per slot, so a request needing more rows than a
- * slot can stage is split across launches. Every result is the same bytes
- * as a lone msbfs_run_ms_bfs / msbfs_run_ms_bfs_stats call.
+ * traversal state is allocated once, and distance rows are staged in one
+ * pool of hbm_budget_bytes shared by all slots; a launch of rows requests
+ * takes only as many lanes as the pool's largest free range holds rows for
+ * (V u32 per lane), reserves those bytes and returns them when it completes,
+ * so a request needing more rows than are free is split across launches.
+ * Every result is the same bytes as a lone msbfs_run_ms_bfs /
+ * msbfs_run_ms_bfs_stats call.
  *
  * Latency: a request of at most small_sources sources is "small". The first
  * express_slots slots take only small requests (at most 2*small_sources
@@ -315,7 +318,7 @@ typedef struct msbfs_server msbfs_server;
 typedef struct msbfs_server_config {
   uint32_t slots;                  /* traversals in flight (0 -> 2)            */
   uint32_t max_sources_per_launch; /* lanes packed per launch (0 -> 512)       */
-  uint64_t hbm_budget_bytes;       /* row staging, all slots (0 -> 8 GiB)      */
+  uint64_t hbm_budget_bytes;       /* row pool of all slots (0 -> 8 GiB)       */
   int method;                      /* engine method (MSBFS_METHOD_AUTO)        */
   uint32_t express_slots;          /* slots reserved for small requests (0)    */
   uint32_t small_sources;          /* small-request threshold (0 -> 64)        */

@@ -171,3 +171,30 @@ def test_server_wait_timeout_and_empty(native, oracle):
         assert_same(res, want, g, src, "rows after an expired wait")
     finally:
         srv.close()
+
+
+def test_server_admits_row_launches_by_free_pool_bytes(native, oracle):
+    """Distance rows are staged in one pool shared by the slots: a launch
+    takes only as many lanes as the largest free range holds rows for. With
+    a pool of 40 lanes' rows and three slots, concurrent row requests of up
+    to 200 sources are cut into launches of at most 40 lanes, and every
+    result is still the oracle's."""
+    g = native.generate_graph500_rmat(11, 8, 81)
+    V = g.num_vertices
+    srv = native.BfsServer(g, slots=3, max_sources_per_launch=512, hbm_budget_bytes=40 * V * 4)
+    try:
+        rng = np.random.default_rng(12)
+        reqs = [rng.integers(0, V, S).astype(np.uint32) for S in (200, 7, 64, 1, 150, 33)]
+        tickets = [srv.submit(r, srv.ROWS) for r in reqs]
+        for r, t in zip(reqs, tickets):
+            res, info = srv.wait(t)
+            assert info["status"] == 0
+            assert info["launches"] >= -(-r.size // 40)
+            assert_same(res, oracle.ms_bfs_fifo(V, g.row_offsets, g.col_indices, r), g, r,
+                        f"{r.size} sources through a 40-lane pool")
+        # statistics need no rows: a request of 300 sources is one launch
+        src = rng.integers(0, V, 300).astype(np.uint32)
+        res, info = srv.wait(srv.submit(src, srv.STATS))
+        assert info["launches"] == 1
+    finally:
+        srv.close()

@@ -52,8 +52,8 @@ struct Slot {
   msbfs_graph* g = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev = nullptr;
-  uint32_t* d_rows = nullptr;
-  size_t rows_cap = 0;  // sources whose rows fit the slot's staging
+  size_t rows_off = 0;    // the running launch's rows in the server's pool
+  size_t rows_bytes = 0;  // (0: none reserved)
   msbfs_source_stats* d_stats = nullptr;
   void* h_stage = nullptr;  // page-locked bounce buffer for pageable outputs
   size_t h_stage_bytes = 0;
@@ -68,6 +68,51 @@ size_t elem_bytes(int mode, size_t V) {
   return mode == MSBFS_SERVE_ROWS ? V * sizeof(uint32_t) : sizeof(msbfs_source_stats);
 }
 
+// First-fit allocator over the server's device pool for distance rows, with
+// coalescing of freed ranges. Admission asks it for the largest free range
+// before packing a launch, so a launch never needs more bytes than exist.
+class RowPool {
+ public:
+  void reset(size_t bytes) {
+    free_.clear();
+    if (bytes) free_[0] = bytes;
+  }
+  size_t largest() const {
+    size_t m = 0;
+    for (const auto& kv : free_) m = std::max(m, kv.second);
+    return m;
+  }
+  bool alloc(size_t bytes, size_t* off) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < bytes) continue;
+      *off = it->first;
+      const size_t rest = it->second - bytes, at = it->first + bytes;
+      free_.erase(it);
+      if (rest) free_[at] = rest;
+      return true;
+    }
+    return false;
+  }
+  void release(size_t off, size_t bytes) {
+    auto it = free_.emplace(off, bytes).first;
+    auto next = std::next(it);
+    if (next != free_.end() && it->first + it->second == next->first) {
+      it->second += next->second;
+      free_.erase(next);
+    }
+    if (it != free_.begin()) {
+      auto prev = std::prev(it);
+      if (prev->first + prev->second == it->first) {
+        prev->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+
+ private:
+  std::map<size_t, size_t> free_;  // offset -> bytes
+};
+
 }  // namespace
 
 struct msbfs_server {
@@ -75,6 +120,8 @@ struct msbfs_server {
   size_t V = 0;
   msbfs_server_config cfg{};
   msbfs_graph* graph = nullptr;  // resident once, owned by slot 0's engine
+  char* d_pool = nullptr;        // hbm_budget_bytes of distance-row staging
+  RowPool pool;
   std::vector<Slot> slots;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -104,8 +151,9 @@ int launch_slot(msbfs_server* s, Slot& sl, const std::vector<uint32_t>& lanes) {
   const size_t V = s->V, n = lanes.size();
   const size_t eb = elem_bytes(sl.mode, V);
   int rc;
+  uint32_t* d_rows = reinterpret_cast<uint32_t*>(s->d_pool + sl.rows_off);
   if (sl.mode == MSBFS_SERVE_ROWS)
-    rc = msbfs_run_ms_bfs_device(sl.eng, s->cfg.method, sl.g, lanes.data(), n, sl.d_rows);
+    rc = msbfs_run_ms_bfs_device(sl.eng, s->cfg.method, sl.g, lanes.data(), n, d_rows);
   else
     rc = msbfs_run_ms_bfs_stats_device(sl.eng, s->cfg.method, sl.g, lanes.data(), n,
                                        sl.d_stats);
@@ -122,7 +170,7 @@ int launch_slot(msbfs_server* s, Slot& sl, const std::vector<uint32_t>& lanes) {
     }
     sl.h_stage_bytes = n * eb;
   }
-  const char* dsrc = sl.mode == MSBFS_SERVE_ROWS ? reinterpret_cast<const char*>(sl.d_rows)
+  const char* dsrc = sl.mode == MSBFS_SERVE_ROWS ? reinterpret_cast<const char*>(d_rows)
                                                  : reinterpret_cast<const char*>(sl.d_stats);
   for (const Part& p : sl.parts) {
     char* dst = p.r->out_pinned ? static_cast<char*>(p.r->out) + p.src_off * eb
@@ -176,15 +224,18 @@ void scheduler(msbfs_server* s) {
         finish_part(s, p, rc);
       }
       sl.parts.clear();
+      if (sl.rows_bytes) s->pool.release(sl.rows_off, sl.rows_bytes);
+      sl.rows_bytes = 0;
       sl.busy = false;
       progress = true;
     }
     // Admissions: the next free slot takes queued requests of one output
-    // mode, in arrival order, until its lanes (and, for rows, its staging
-    // bytes) are used up; larger requests continue in later launches. An
-    // express slot takes small requests only; a general slot takes large
-    // requests first when express slots exist, small ones only when no large
-    // request waits.
+    // mode, in arrival order, until its lanes are used up -- and, for rows,
+    // until the lanes' rows (V u32 each) fill the largest free range of the
+    // server's row pool, which the launch then reserves until it completes;
+    // larger requests continue in later launches. An express slot takes
+    // small requests only; a general slot takes large requests first when
+    // express slots exist, small ones only when no large request waits.
     const size_t small = s->cfg.small_sources;
     for (Slot& sl : s->slots) {
       if (sl.busy || s->queue.empty()) continue;
@@ -206,7 +257,11 @@ void scheduler(msbfs_server* s) {
       sl.mode = head->mode;
       size_t cap = s->cfg.max_sources_per_launch;
       if (sl.express) cap = std::min(cap, 2 * small);
-      if (sl.mode == MSBFS_SERVE_ROWS) cap = std::min(cap, sl.rows_cap);
+      const size_t row_bytes = s->V * sizeof(uint32_t);
+      if (sl.mode == MSBFS_SERVE_ROWS) {
+        cap = std::min(cap, s->pool.largest() / row_bytes);
+        if (cap == 0) continue;  // rows of a single lane do not fit until a launch completes
+      }
       std::vector<uint32_t> lanes;
       const auto now = Clock::now();
       for (size_t i = 0; i < s->queue.size() && lanes.size() < cap;) {
@@ -239,11 +294,19 @@ void scheduler(msbfs_server* s) {
         else
           ++i;
       }
+      // The pool's largest range held `cap` lanes' rows a moment ago and
+      // only this thread allocates, so the reservation succeeds.
+      bool reserved = true;
+      sl.rows_bytes = 0;
+      if (sl.mode == MSBFS_SERVE_ROWS) {
+        reserved = s->pool.alloc(lanes.size() * row_bytes, &sl.rows_off);
+        if (reserved) sl.rows_bytes = lanes.size() * row_bytes;
+      }
       sl.busy = true;
       any_busy = true;
       progress = true;
       lk.unlock();
-      sl.launch_rc = launch_slot(s, sl, lanes);
+      sl.launch_rc = reserved ? launch_slot(s, sl, lanes) : MSBFS_ERR_OOM;
       lk.lock();
     }
     if (s->stop && s->queue.empty() && !any_busy) break;
@@ -259,9 +322,10 @@ void destroy_slots(msbfs_server* s) {
   // The shared graph goes first: it drops every attached engine's workspaces.
   if (s->graph) msbfs_graph_destroy(s->graph);
   s->graph = nullptr;
+  if (s->d_pool) cudaFree(s->d_pool);
+  s->d_pool = nullptr;
   for (Slot& sl : s->slots) {
     if (sl.eng) msbfs_engine_destroy(sl.eng);
-    if (sl.d_rows) cudaFree(sl.d_rows);
     if (sl.d_stats) cudaFree(sl.d_stats);
     if (sl.h_stage) cudaFreeHost(sl.h_stage);
     if (sl.ev) cudaEventDestroy(sl.ev);
@@ -299,9 +363,13 @@ int msbfs_server_create(int device, size_t V, size_t E, const uint32_t* ro, cons
   }
   int prio_low = 0, prio_high = 0;
   cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-  const size_t per_slot = s->cfg.hbm_budget_bytes / s->cfg.slots;
-  const size_t rows_cap =
-      std::max<size_t>(1, std::min<size_t>(s->cfg.max_sources_per_launch, per_slot / (V * 4)));
+  // The row pool holds at least one lane's rows.
+  const size_t pool_bytes = std::max<size_t>(s->cfg.hbm_budget_bytes / (V * 4), 1) * V * 4;
+  if (cudaMalloc((void**)&s->d_pool, pool_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return MSBFS_ERR_OOM;
+  }
+  s->pool.reset(pool_bytes);
   s->slots.resize(s->cfg.slots);
   int rc = MSBFS_OK;
   for (size_t k = 0; k < s->slots.size(); ++k) {
@@ -322,9 +390,7 @@ int msbfs_server_create(int device, size_t V, size_t E, const uint32_t* ro, cons
     if (k == 0 && (rc = msbfs_graph_create(sl.eng, V, E, ro, ci, &s->graph))) break;
     if ((rc = msbfs_graph_attach(s->graph, sl.eng))) break;
     sl.g = s->graph;
-    sl.rows_cap = rows_cap;
-    if (cudaMalloc((void**)&sl.d_rows, rows_cap * V * 4) != cudaSuccess ||
-        cudaMalloc((void**)&sl.d_stats,
+    if (cudaMalloc((void**)&sl.d_stats,
                    s->cfg.max_sources_per_launch * sizeof(msbfs_source_stats)) != cudaSuccess) {
       cudaGetLastError();
       rc = MSBFS_ERR_OOM;
