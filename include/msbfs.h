@@ -170,7 +170,7 @@ int msbfs_engine_set_tuning(msbfs_engine *engine, uint32_t max_words_per_pass,
  * settings. Calls that the router sends to the CTA-per-source path are not
  * tuned (the settings do not apply to it). */
 typedef struct msbfs_tuning {
-  uint32_t max_words_per_pass; /* u32 words per vertex of a pass (32 sources each) */
+  uint32_t max_words_per_pass; /* u32 words per vertex of this call's passes       */
   uint32_t alpha;              /* top-down -> bottom-up: frontier out-edges * alpha > E */
   uint32_t beta;               /* bottom-up -> top-down: frontier vertices * beta < V  */
   uint32_t hub_split;          /* in-edge slice length of bottom-up steps              */

@@ -1358,7 +1358,11 @@ extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint
   std::strncpy(t.class_name, key.c_str(), sizeof t.class_name - 1);
   LevelSettings best{e->max_words, e->alpha, e->beta, g->split, e->bits_div};
   auto report = [&](const LevelSettings& s) {
-    t.max_words_per_pass = s.words;
+    // The words a pass of this call uses (a cap above the sources' need
+    // makes no difference).
+    uint32_t need = 1;
+    while (need < (S + 31) / 32 && need < 64) need <<= 1;
+    t.max_words_per_pass = std::min(s.words, need);
     t.alpha = s.alpha;
     t.beta = s.beta;
     t.hub_split = s.split;
