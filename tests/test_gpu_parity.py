@@ -369,3 +369,48 @@ def test_autotune_same_bytes_and_cache(native, oracle, tmp_path):
         assert len(open(cache).read().splitlines()) == 1
     finally:
         eng.close()
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_byte_row_transport_mixed_passes(native, oracle, monkeypatch, pinned):
+    """Rows bound for pageable host memory travel as one byte per distance
+    when every distance of a pass is below 255 and are widened on the host;
+    deeper passes keep u32 rows (page-locked output always gets u32 rows
+    written over the link). A graph of an R-MAT component beside a path of
+    400 vertices, with passes of 32 sources: the first pass's sources sit
+    in the R-MAT part (byte rows), the second's include the path's end
+    (levels up to 399, u32 rows). Rows equal the oracle's and those of an
+    engine that never narrows (MSBFS_NARROW=0), for pageable and
+    page-locked output."""
+    torch = pytest.importorskip("torch")
+    r = native.generate_graph500_rmat(10, 8, 17)
+    n0 = r.num_vertices
+    edges = [(u, int(v)) for u in range(n0) for v in r.neighbors(u)]
+    edges += [(n0 + i, n0 + i + 1) for i in range(399)]
+    edges += [(n0 + i + 1, n0 + i) for i in range(399)]
+    g = native.CsrGraph.from_edge_list(n0 + 400, edges)
+    deg = np.diff(r.row_offsets.astype(np.int64))
+    live = np.flatnonzero(deg > 0).astype(np.uint32)
+    src = np.concatenate([live[:32], live[32:60], np.array([n0, n0 + 399, n0 + 7, n0 + 200],
+                                                           np.uint32)]).astype(np.uint32)
+    want = _oracle(oracle, g, src)
+    outs = {}
+    for narrow in ("1", "0"):
+        monkeypatch.setenv("MSBFS_NARROW", narrow)
+        eng = native.GpuBfsEngine(native.GpuBfsMethod.PushPullAdaptive)
+        try:
+            eng.set_tuning(max_words_per_pass=1)
+            if pinned:
+                buf = torch.empty(src.size * g.num_vertices, dtype=torch.int32, pin_memory=True)
+                out = buf.numpy().view(np.uint32)
+                out[:] = 7
+                eng.run_ms_bfs_into(g, src, out)
+                out = out.copy()
+            else:
+                out = eng.run_ms_bfs(g, src)
+            assert eng.last_stats["passes"] == 2 and eng.last_stats["levels"] >= 399
+        finally:
+            eng.close()
+        assert_same(out, want, g, src, f"narrow={narrow} pinned={pinned}")
+        outs[narrow] = out
+    assert np.array_equal(outs["1"], outs["0"])

@@ -65,6 +65,7 @@ struct LevelCtl {
   unsigned long long c_rows;
   unsigned long long t_start;    // min %globaltimer over the level's blocks
   uint32_t use_bits;             // bottom-up step checks frontier bitmaps first
+  uint32_t narrow;               // the pass's rows went to PassDesc::dist8 as bytes
   // Vertex-tile cursors of the running bottom-up step: the work list is cut
   // into WORK_STRIPES contiguous stripes, each with its own cursor on its own
   // 128-byte line, so the claims of a level spread over several L2 slices
@@ -102,6 +103,10 @@ struct PassDesc {
   uint32_t* dist;           // first row of this pass in the distance matrix
   uint32_t* reach;          // non-null: write visited words here instead
   SourceStats* stats;       // non-null: per-source reductions instead of rows
+  // Non-null: when every distance of the pass is below 255, the rows are
+  // written here as one byte per distance (0xFF = unreachable) instead of
+  // into `dist`, and LevelCtl::narrow is set; the host widens them.
+  uint8_t* dist8;
   uint32_t num_sources;     // P
   uint32_t reach_wpv;       // words per vertex of the reachability output
   uint32_t reach_col;       // word column of this pass in that output

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -24,6 +25,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -159,6 +161,7 @@ struct msbfs_engine {
   uint32_t level_cap = 0;   // levels per pass before MSBFS_ERR_TIMEOUT (0: V + 2)
   bool host_loop = false;
   bool zero_copy = true;  // MSBFS_ZERO_COPY=0 stages host output in HBM instead
+  bool narrow = true;     // MSBFS_NARROW=0 keeps host-bound rows u32 over the link
   int profiling = 0;
   std::vector<msbfs_level_record> log;       // records of the last call
   LevelRec* h_log = nullptr;                 // pinned, LOG_CAP per pass
@@ -171,6 +174,11 @@ struct msbfs_engine {
   size_t d_sources_cap = 0;
   uint32_t* d_dist = nullptr;
   size_t d_dist_cap = 0;  // u32 elements
+  uint8_t* d_dist8 = nullptr;  // byte rows of host-bound calls
+  size_t d_dist8_cap = 0;
+  uint8_t* h_dist8 = nullptr;  // page-locked landing buffer of the byte rows
+  size_t h_dist8_cap = 0;
+  std::vector<cudaEvent_t> chunk_events;  // one per landed chunk of byte rows
   uint32_t* d_reach = nullptr;
   size_t d_reach_cap = 0;
   uint32_t* d_cta_queue = nullptr;
@@ -578,7 +586,8 @@ int resolve_method(const msbfs_graph* g, int method, size_t S) {
 // copy stream while later passes run.
 int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t* sources,
                  size_t S, uint32_t* dist_dev, uint32_t* reach_dev, uint32_t* host_out,
-                 uint32_t* host_reach, SourceStats* stats_dev = nullptr) {
+                 uint32_t* host_reach, SourceStats* stats_dev = nullptr,
+                 uint8_t* dist8_dev = nullptr) {
   int rc;
   if (stats_dev) CK(cudaMemsetAsync(stats_dev, 0, S * sizeof(SourceStats), eng->stream));
   const int m = resolve_method(g, method, S);
@@ -686,6 +695,7 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     d.dist = dist_dev ? dist_dev + s0 * V : nullptr;
     d.reach = reach_dev;
     d.stats = stats_dev ? stats_dev + s0 : nullptr;
+    d.dist8 = dist8_dev ? dist8_dev + s0 * V : nullptr;
     d.num_sources = (uint32_t)np;
     d.reach_wpv = (uint32_t)wpv;
     d.reach_col = (uint32_t)(ps * W);
@@ -925,6 +935,99 @@ void free_graph(msbfs_graph* g) {
   delete g;
 }
 
+// Copies n byte distances from the device to the host through a ring of
+// page-locked chunk slots (one event per slot on the copy stream) while
+// every hardware thread widens each chunk, once it has landed, into u32
+// (0xFF -> 0xFFFFFFFF) at `out`: the host link carries a quarter of the
+// bytes, and the host's cores, which write memory faster than the link
+// delivers it, do the widening. The calling thread issues the copies; a
+// slot is refilled only after all workers have widened its previous chunk,
+// and a worker waits for its chunk's copy to be issued before it waits on
+// the slot's event.
+int widen_to_host(msbfs_engine* eng, const uint8_t* src, uint32_t* out, size_t n) {
+  if (n == 0) return MSBFS_OK;
+  constexpr size_t CHUNK = 32u << 20, SLOTS = 16;
+  const size_t stage = std::min(n, CHUNK * SLOTS);
+  if (stage > eng->h_dist8_cap) {
+    if (eng->h_dist8) cudaFreeHost(eng->h_dist8);
+    eng->h_dist8 = nullptr;
+    eng->h_dist8_cap = 0;
+    CK(cudaHostAlloc((void**)&eng->h_dist8, stage, cudaHostAllocDefault));
+    eng->h_dist8_cap = stage;
+  }
+  while (eng->chunk_events.size() < SLOTS) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    eng->chunk_events.push_back(e);
+  }
+  const size_t nchunks = (n + CHUNK - 1) / CHUNK;
+  const unsigned T = std::max(1u, std::thread::hardware_concurrency());
+  std::mutex mu;
+  std::condition_variable cv;
+  size_t issued = 0, widened = 0;  // chunks issued / widened by every worker (in order)
+  unsigned slot_done[SLOTS] = {};
+  bool failed = false;
+  const uint8_t* ring = eng->h_dist8;
+  std::vector<std::thread> workers;
+  for (unsigned k = 0; k < T; ++k) {
+    workers.emplace_back([&, k] {
+      cudaSetDevice(eng->device);
+      for (size_t c = 0; c < nchunks; ++c) {
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return issued > c || failed; });
+          if (failed) return;
+        }
+        const size_t slot = c % SLOTS;
+        if (cudaEventSynchronize(eng->chunk_events[slot]) != cudaSuccess) {
+          std::lock_guard<std::mutex> lk(mu);
+          failed = true;
+          cv.notify_all();
+          return;
+        }
+        const size_t b = c * CHUNK, len = std::min(CHUNK, n - b);
+        const size_t lo = len * k / T, hi = len * (k + 1) / T;
+        const uint8_t* in = ring + slot * CHUNK;
+        uint32_t* o = out + b;
+        for (size_t i = lo; i < hi; ++i) {
+          const uint32_t d = in[i];
+          o[i] = d == 0xFFu ? 0xFFFFFFFFu : d;
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        if (++slot_done[slot] == T) {
+          slot_done[slot] = 0;
+          ++widened;
+          cv.notify_all();
+        }
+      }
+    });
+  }
+  cudaError_t err = cudaSuccess;
+  for (size_t c = 0; c < nchunks && err == cudaSuccess; ++c) {
+    const size_t slot = c % SLOTS, b = c * CHUNK, len = std::min(CHUNK, n - b);
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return c < SLOTS || widened + SLOTS > c || failed; });
+      if (failed) break;
+    }
+    err = cudaMemcpyAsync(eng->h_dist8 + slot * CHUNK, src + b, len, cudaMemcpyDeviceToHost,
+                          eng->copy_stream);
+    if (err == cudaSuccess) err = cudaEventRecord(eng->chunk_events[slot], eng->copy_stream);
+    std::lock_guard<std::mutex> lk(mu);
+    if (err == cudaSuccess)
+      issued = c + 1;
+    else
+      failed = true;
+    cv.notify_all();
+  }
+  for (std::thread& t : workers) t.join();
+  if (failed || err != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(eng, MSBFS_ERR_CUDA, "byte-row copy failed");
+  }
+  return MSBFS_OK;
+}
+
 // Blocking run into caller-owned host memory.
 int run_host(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t* sources,
              size_t S, uint32_t* out, msbfs_stats* stats) {
@@ -940,18 +1043,51 @@ int run_host(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t
   // CTA-per-source path stores 4-byte distances as it discovers them, which
   // the host link serves ~9x slower than a staged copy, so it keeps staging.
   const bool cta = method_path(resolve_method(g, method, S)) == MSBFS_PATH_CTA;
+  const size_t V = g->V;
+  uint32_t* zc = nullptr;  // device address of page-locked `out`
   if (eng->zero_copy && !cta) {
     cudaPointerAttributes attr{};
     if (cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
-        attr.type == cudaMemoryTypeHost && attr.devicePointer) {
-      if ((rc = enqueue_call(eng, method, g, sources, S, (uint32_t*)attr.devicePointer, nullptr,
-                             nullptr, nullptr)))
-        return rc;
-      return finish_call(eng, stats);
-    }
-    cudaGetLastError();
+        attr.type == cudaMemoryTypeHost && attr.devicePointer)
+      zc = (uint32_t*)attr.devicePointer;
+    else
+      cudaGetLastError();
   }
-  const size_t total = S * g->V;
+  // Pageable output: byte rows for every pass whose distances all fit a
+  // byte (decided on the device), widened by the host's cores; a deeper
+  // pass writes u32 rows to HBM staging, copied afterwards. Without room for
+  // the byte rows the call keeps u32 rows throughout. Page-locked output
+  // keeps u32 rows written straight over the link: there the link alone is
+  // faster than link + widening, which share the host's memory bandwidth.
+  if (eng->narrow && !cta && !zc &&
+      grow(eng, &eng->d_dist8, &eng->d_dist8_cap, S * V) == MSBFS_OK) {
+    uint32_t* wide = zc;
+    if (!wide) {
+      if ((rc = grow(eng, &eng->d_dist, &eng->d_dist_cap, S * V))) return rc;
+      wide = eng->d_dist;
+    }
+    if ((rc = enqueue_call(eng, method, g, sources, S, wide, nullptr, nullptr, nullptr, nullptr,
+                           eng->d_dist8)))
+      return rc;
+    if ((rc = finish_call(eng, stats))) return rc;
+    const size_t PW = (size_t)eng->last.words_per_vertex * 32;
+    for (size_t ps = 0; ps < eng->last_passes; ++ps) {
+      const size_t s0 = ps * PW, np = std::min(PW, S - s0);
+      if (eng->h_ctl[ps].narrow) {
+        if ((rc = widen_to_host(eng, eng->d_dist8 + s0 * V, out + s0 * V, np * V))) return rc;
+      } else if (!zc) {
+        CK(cudaMemcpy(out + s0 * V, eng->d_dist + s0 * V, np * V * sizeof(uint32_t),
+                      cudaMemcpyDeviceToHost));
+      }
+    }
+    return MSBFS_OK;
+  }
+  if (zc) {
+    if ((rc = enqueue_call(eng, method, g, sources, S, zc, nullptr, nullptr, nullptr)))
+      return rc;
+    return finish_call(eng, stats);
+  }
+  const size_t total = S * V;
   if ((rc = grow(eng, &eng->d_dist, &eng->d_dist_cap, total))) return rc;
   if ((rc = enqueue_call(eng, method, g, sources, S, eng->d_dist, nullptr, out, nullptr)))
     return rc;
@@ -993,6 +1129,8 @@ int msbfs_engine_create(int device, int method, msbfs_engine** out) {
   e->host_loop = hl && hl[0] == '1';
   const char* zc = getenv("MSBFS_ZERO_COPY");
   e->zero_copy = !(zc && zc[0] == '0');
+  const char* nr = getenv("MSBFS_NARROW");
+  e->narrow = !(nr && nr[0] == '0');
   *out = eng.release();
   return MSBFS_OK;
 }
@@ -1005,6 +1143,9 @@ void msbfs_engine_destroy(msbfs_engine* e) {
   e->ws.clear();
   cudaFree(e->d_sources);
   cudaFree(e->d_dist);
+  cudaFree(e->d_dist8);
+  if (e->h_dist8) cudaFreeHost(e->h_dist8);
+  for (cudaEvent_t ev : e->chunk_events) cudaEventDestroy(ev);
   cudaFree(e->d_reach);
   cudaFree(e->d_cta_queue);
   cudaFree(e->d_cta_bits);

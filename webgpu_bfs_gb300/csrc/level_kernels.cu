@@ -1030,6 +1030,7 @@ struct MatOut {
   uint32_t* dist;
   uint32_t* reach;
   uint32_t reach_wpv, reach_col;
+  uint8_t* dist8;  // non-null: rows as one byte per distance (all below 255)
 };
 
 // Writes the rows of column cs of the staged tile: word cw = g*TW + c of the
@@ -1079,9 +1080,32 @@ __device__ __forceinline__ void mat_column(const LevelParams& p, const MatOut& o
       if (vl + t < V) out.reach[(size_t)(vl + t) * out.reach_wpv + out.reach_col + cw] = xs[t];
     return;
   }
-  uint32_t* dist = out.dist;
   const uint32_t s0 = cw * 32;
   const uint32_t jn = min(32u, P - s0);
+  if (out.dist8) {
+    // Byte rows: no lane is deeper than the planes here (every distance is
+    // below 255), so there is no ovf lane to skip.
+    for (uint32_t j = 0; j < jn; ++j) {
+      uint8_t dv[2];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        uint32_t val = 0;
+#pragma unroll
+        for (int b = 0; b < NPU; ++b) val |= ((pl[b][t] >> j) & 1u) << b;
+        dv[t] = ((xs[t] >> j) & 1u) ? (uint8_t)val : (uint8_t)0xFF;
+      }
+      uint8_t* row = out.dist8 + (size_t)(s0 + j) * V + vl;
+      if (vec_ok && vl + 1 < V) {
+        *reinterpret_cast<uchar2*>(row) = make_uchar2(dv[0], dv[1]);
+      } else {
+#pragma unroll
+        for (int t = 0; t < 2; ++t)
+          if (vl + t < V) row[t] = dv[t];
+      }
+    }
+    return;
+  }
+  uint32_t* dist = out.dist;
   const bool any_ovf = (ov[0] | ov[1]) != 0;
   const bool full = vec_ok && vl + 1 < V;
   for (uint32_t j = 0; j < jn; ++j) {
@@ -1256,13 +1280,19 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(
   const uint32_t dmax = p.ctl->level;
   const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
   const bool use_ovf = dmax >= (1u << p.NP);
-  const MatOut out{dsc->dist, dsc->reach, dsc->reach_wpv, dsc->reach_col};
+  // Byte rows when the pass asks for them and every distance fits a byte
+  // (0xFF is kept for unreachable); the control block tells the host.
+  const bool narrow = dsc->dist8 && !dsc->reach && dmax < 255u;
+  if (narrow && blockIdx.x == 0 && threadIdx.x == 0) p.ctl->narrow = 1;
+  const MatOut out{dsc->dist, dsc->reach, dsc->reach_wpv, dsc->reach_col,
+                   narrow ? dsc->dist8 : nullptr};
   const uint32_t V = p.V;
   const size_t VW = (size_t)V * W;
   const uint32_t tid = threadIdx.x;
   const uint32_t lane = tid & 31;
   const uint32_t warp = tid >> 5;
-  const bool vec_ok = (V % 2 == 0) && (((uintptr_t)out.dist & 7) == 0);
+  const bool vec_ok = narrow ? (V % 2 == 0) && (((uintptr_t)out.dist8 & 1) == 0)
+                             : (V % 2 == 0) && (((uintptr_t)out.dist & 7) == 0);
   const uint32_t ngu = (Wu + G::TW - 1) / G::TW;  // word groups in use
   const size_t nitems = (size_t)((V + G::TV - 1) / G::TV) * ngu;
   const uint32_t o = 4 * tid;  // tile word offset of this thread's four words
