@@ -484,6 +484,18 @@ def run_ours(args, spec):
     host_out = None
     try:
         host_out = torch.empty(S * V, dtype=torch.int32, pin_memory=True)
+        # The host link's ceiling for the step's rows: one device-to-host
+        # copy of as many bytes into the same page-locked buffer (before the
+        # e2e calls, which then overwrite the buffer with their rows).
+        dev = torch.zeros(S * V, dtype=torch.int32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(2):
+            e0.record()
+            host_out.copy_(dev, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+        link_ms = e0.elapsed_time(e1)
+        del dev
         host_src = torch.from_numpy(src.astype(np.int32)).pin_memory()
         hs = host_src.numpy().view(np.uint32)
         ho = host_out.numpy().view(np.uint32)
@@ -501,6 +513,8 @@ def run_ours(args, spec):
         e2e = {"value": world * S * args.steps / dt, "unit": "sources/s",
                "h2d_bytes_per_step": int(S * 4), "d2h_bytes_per_step": int(S * V * 4),
                "ms_per_step": 1000 * dt / args.steps,
+               "link_d2h_gbs": S * V * 4 / (link_ms / 1000.0) / 1e9,
+               "link_floor_ms": link_ms,
                "note": "graph resident (uploaded once); per step: sources H2D, BFS, "
                        "S*V u32 distances D2H into pinned host memory"}
     except Exception as ex:  # pragma: no cover - reported, not hidden

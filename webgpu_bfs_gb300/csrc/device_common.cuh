@@ -110,7 +110,8 @@ struct PassDesc {
   uint32_t num_sources;     // P
   uint32_t reach_wpv;       // words per vertex of the reachability output
   uint32_t reach_col;       // word column of this pass in that output
-  uint32_t pad;
+  uint32_t row_split;       // split materialisation: rows below go u32 to dist,
+                            // rows from it on as bytes to dist8 (multiple of 32)
 };
 
 struct LevelParams {
@@ -183,8 +184,14 @@ constexpr uint32_t DIR_BOTH = 2;
 void launch_level(const LevelParams& p, const LevelKernelInfo& k, uint32_t dir, bool count,
                   cudaStream_t s);
 // reduce: per-source reductions (reduce_kernel) instead of rows or bitmasks.
+// phase (materialisation only): MAT_ALL writes every row (bytes when the
+// pass allows) and clears the traversal state; MAT_BYTES writes only the
+// byte rows from PassDesc::row_split on and clears nothing (nothing at all
+// unless every distance fits a byte); MAT_WIDE then writes the u32 rows
+// below the split (all rows when the pass did not go to bytes) and clears.
+enum : uint32_t { MAT_BYTES = 0, MAT_WIDE = 1, MAT_ALL = 2 };
 void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
-                        cudaStream_t s);
+                        cudaStream_t s, uint32_t phase = MAT_ALL);
 void launch_cleanup(const LevelParams& p, cudaStream_t s);
 
 struct CtaParams {

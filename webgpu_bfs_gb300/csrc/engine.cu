@@ -89,12 +89,12 @@ struct Workspace {
   // buffers may hold that pass's bits, so the next call builds a fresh
   // workspace instead of reusing this one.
   bool dirty = false;
-  // One instantiated pass per finishing kernel: [0] materialise, [1] reduce
-  // (built on first use).
-  cudaGraph_t graph[2] = {nullptr, nullptr};
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  // One instantiated pass per ending: [0] materialise, [1] reduce, [2] the
+  // byte rows of a split materialisation only (built on first use).
+  cudaGraph_t graph[3] = {nullptr, nullptr, nullptr};
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
   ~Workspace() {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
       if (exec[i]) cudaGraphExecDestroy(exec[i]);
       if (graph[i]) cudaGraphDestroy(graph[i]);
     }
@@ -179,6 +179,13 @@ struct msbfs_engine {
   uint8_t* h_dist8 = nullptr;  // page-locked landing buffer of the byte rows
   size_t h_dist8_cap = 0;
   std::vector<cudaEvent_t> chunk_events;  // one per landed chunk of byte rows
+  // Page-locked output: share of a pass's rows written as u32 over the link
+  // (MSBFS_SPLIT_ROWS; R-MAT 22, S=512: 1.0 50.5 ms per call, 0.8 47.0,
+  // 0.7 45.8, 0.6 44.0, 0.5 ~45).
+  double split_frac = 0.6;
+  bool last_split = false;   // the last call split its materialisation
+  std::vector<uint32_t> split_rows;         // per pass: first byte row
+  std::vector<cudaEvent_t> split_events;    // per pass: its byte rows are done
   uint32_t* d_reach = nullptr;
   size_t d_reach_cap = 0;
   uint32_t* d_cta_queue = nullptr;
@@ -241,12 +248,15 @@ int dev_alloc(msbfs_engine* eng, Workspace* w, void** ptr, size_t bytes) {
   return MSBFS_OK;
 }
 
-// reduce: the pass ends in reduce_kernel (per-source reductions) instead of
-// materialize_kernel.
-int build_graph_exec(msbfs_engine* eng, Workspace* w, bool reduce) {
+// The pass ends in materialize_kernel (variant 0), reduce_kernel (1,
+// per-source reductions) or, for a split materialisation, the byte-row
+// phase alone (2: the host then launches the u32 phase and the cleanup).
+enum : int { PASS_ROWS = 0, PASS_STATS = 1, PASS_BYTES = 2 };
+int build_graph_exec(msbfs_engine* eng, Workspace* w, int variant) {
+  const bool reduce = variant == PASS_STATS;
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
-  w->graph[reduce] = g;
+  w->graph[variant] = g;
   cudaGraphNode_t n_mctl, n_mst, n_init, n_cond, n_lvl, n_mat, n_clean;
   cudaMemsetParams m1{};
   m1.dst = w->d_ctl;
@@ -321,25 +331,29 @@ int build_graph_exec(msbfs_engine* eng, Workspace* w, bool reduce) {
     CK(cudaGraphAddKernelNode(&n_lvl, body, prev ? &prev : nullptr, prev ? 1 : 0, &kl));
   }
 
+  uint32_t phase = variant == PASS_BYTES ? MAT_BYTES : MAT_ALL;
+  void* args_m[] = {&w->p, &phase};
   cudaKernelNodeParams km{};
   km.func = reduce ? w->k.reduce : w->k.materialize;
   km.gridDim = dim3(reduce ? w->k.red_grid : w->k.mat_grid);
   km.blockDim = dim3(reduce ? w->k.red_block : w->k.mat_block);
   km.sharedMemBytes = reduce ? 0u : (unsigned)w->k.mat_smem;
-  km.kernelParams = args_p;
+  km.kernelParams = reduce ? args_p : args_m;
   CK(cudaGraphAddKernelNode(&n_mat, g, &n_cond, 1, &km));
 
-  cudaKernelNodeParams kc{};
-  kc.func = w->k.cleanup;
-  kc.gridDim = dim3(256);
-  kc.blockDim = dim3(256);
-  kc.sharedMemBytes = 0;
-  kc.kernelParams = args_p;
-  CK(cudaGraphAddKernelNode(&n_clean, g, &n_cond, 1, &kc));
+  if (variant != PASS_BYTES) {
+    cudaKernelNodeParams kc{};
+    kc.func = w->k.cleanup;
+    kc.gridDim = dim3(256);
+    kc.blockDim = dim3(256);
+    kc.sharedMemBytes = 0;
+    kc.kernelParams = args_p;
+    CK(cudaGraphAddKernelNode(&n_clean, g, &n_cond, 1, &kc));
+  }
   (void)n_lvl;
   (void)n_mat;
   (void)n_clean;
-  CK(cudaGraphInstantiate(&w->exec[reduce], g, 0));
+  CK(cudaGraphInstantiate(&w->exec[variant], g, 0));
   return MSBFS_OK;
 }
 
@@ -439,7 +453,7 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   if ((rc = dev_alloc(eng, w.get(), &ptr, (size_t)std::max(p.hlive_words, 1u) * 4))) return rc;
   p.hlive = (uint32_t*)ptr;
   if (!eng->host_loop) {
-    rc = build_graph_exec(eng, w.get(), false);
+    rc = build_graph_exec(eng, w.get(), PASS_ROWS);
     if (rc) {
       // Conditional graph nodes unavailable: fall back to the host-driven loop.
       eng->host_loop = true;
@@ -587,7 +601,7 @@ int resolve_method(const msbfs_graph* g, int method, size_t S) {
 int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t* sources,
                  size_t S, uint32_t* dist_dev, uint32_t* reach_dev, uint32_t* host_out,
                  uint32_t* host_reach, SourceStats* stats_dev = nullptr,
-                 uint8_t* dist8_dev = nullptr) {
+                 uint8_t* dist8_dev = nullptr, double split_frac = 0.0) {
   int rc;
   if (stats_dev) CK(cudaMemsetAsync(stats_dev, 0, S * sizeof(SourceStats), eng->stream));
   const int m = resolve_method(g, method, S);
@@ -657,9 +671,25 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
   if ((rc = get_workspace(eng, g, W, mode, &w))) return rc;
   const bool reduce = stats_dev != nullptr;
   if (reduce && !eng->host_loop && w->exec[0] && !w->exec[1] &&
-      build_graph_exec(eng, w, true) != MSBFS_OK) {
+      build_graph_exec(eng, w, PASS_STATS) != MSBFS_OK) {
     eng->host_loop = true;
     cudaGetLastError();
+  }
+  // Split materialisation (graph loop only): the pass's graph ends after
+  // the byte rows; the u32 rows and the cleanup follow as plain launches
+  // while the host widens the bytes.
+  bool split = split_frac > 0.0 && dist8_dev && dist_dev && !reduce && !reach_dev &&
+               eng->profiling == 0 && !eng->host_loop && w->exec[PASS_ROWS];
+  if (split && !w->exec[PASS_BYTES] && build_graph_exec(eng, w, PASS_BYTES) != MSBFS_OK) {
+    cudaGetLastError();
+    split = false;
+  }
+  eng->last_split = split;
+  eng->split_rows.assign(passes, 0);
+  while (split && eng->split_events.size() < passes) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    eng->split_events.push_back(e);
   }
   if (passes > eng->h_ctl_cap) {
     CK(cudaStreamSynchronize(eng->stream));
@@ -699,11 +729,21 @@ int enqueue_call(msbfs_engine* eng, int method, const msbfs_graph* g, const uint
     d.num_sources = (uint32_t)np;
     d.reach_wpv = (uint32_t)wpv;
     d.reach_col = (uint32_t)(ps * W);
+    d.row_split = split ? (uint32_t)(split_frac * (double)np) / 32u * 32u : 0u;
+    eng->split_rows[ps] = d.row_split;
     // Pageable source: the copy is staged before the call returns, so the
     // stack descriptor can go out of scope.
     CK(cudaMemcpyAsync(w->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, eng->stream));
     if (eng->profiling >= 2) {
       if ((rc = run_pass_profiled(eng, w, reduce, &eng->pass_event_ms[ps]))) return rc;
+    } else if (split) {
+      CK(cudaGraphLaunch(w->exec[PASS_BYTES], eng->stream));
+      CK(cudaMemcpyAsync(&eng->h_ctl[ps], w->d_ctl, sizeof(LevelCtl), cudaMemcpyDeviceToHost,
+                         eng->stream));
+      CK(cudaEventRecord(eng->split_events[ps], eng->stream));
+      launch_materialize(w->p, w->k, false, eng->stream, MAT_WIDE);
+      launch_cleanup(w->p, eng->stream);
+      CK(cudaGetLastError());
     } else if (w->exec[reduce] && !eng->host_loop) {
       CK(cudaGraphLaunch(w->exec[reduce], eng->stream));
     } else {
@@ -1053,24 +1093,39 @@ int run_host(msbfs_engine* eng, int method, const msbfs_graph* g, const uint32_t
     else
       cudaGetLastError();
   }
-  // Pageable output: byte rows for every pass whose distances all fit a
-  // byte (decided on the device), widened by the host's cores; a deeper
-  // pass writes u32 rows to HBM staging, copied afterwards. Without room for
-  // the byte rows the call keeps u32 rows throughout. Page-locked output
-  // keeps u32 rows written straight over the link: there the link alone is
-  // faster than link + widening, which share the host's memory bandwidth.
-  if (eng->narrow && !cta && !zc &&
-      grow(eng, &eng->d_dist8, &eng->d_dist8_cap, S * V) == MSBFS_OK) {
+  // Byte rows (decided on the device for each pass: all its distances fit a
+  // byte) widened by the host's cores. Pageable output: a byte pass's rows
+  // all travel as bytes; a deeper pass writes u32 rows to HBM staging,
+  // copied afterwards. Page-locked output: the link alone is about as fast
+  // as link + widening, which share the host's memory bandwidth, so a pass
+  // splits its rows -- the first split_frac written as u32 straight over the
+  // link while the host widens the rest, which travel as bytes. Without room
+  // for the byte rows the call keeps u32 rows throughout.
+  const bool use_bytes = eng->narrow && !cta && (!zc || eng->split_frac < 1.0);
+  if (use_bytes && grow(eng, &eng->d_dist8, &eng->d_dist8_cap, S * V) == MSBFS_OK) {
     uint32_t* wide = zc;
     if (!wide) {
       if ((rc = grow(eng, &eng->d_dist, &eng->d_dist_cap, S * V))) return rc;
       wide = eng->d_dist;
     }
     if ((rc = enqueue_call(eng, method, g, sources, S, wide, nullptr, nullptr, nullptr, nullptr,
-                           eng->d_dist8)))
+                           eng->d_dist8, zc ? eng->split_frac : 0.0)))
       return rc;
-    if ((rc = finish_call(eng, stats))) return rc;
     const size_t PW = (size_t)eng->last.words_per_vertex * 32;
+    if (eng->last_split) {
+      // Each pass's bytes are widened as soon as they exist, while the GPU
+      // writes its u32 rows and runs later passes.
+      for (size_t ps = 0; ps < eng->last_passes; ++ps) {
+        CK(cudaEventSynchronize(eng->split_events[ps]));
+        if (!eng->h_ctl[ps].narrow) continue;
+        const size_t s0 = ps * PW, np = std::min(PW, S - s0), r0 = eng->split_rows[ps];
+        if ((rc = widen_to_host(eng, eng->d_dist8 + (s0 + r0) * V, out + (s0 + r0) * V,
+                                (np - r0) * V)))
+          return rc;
+      }
+      return finish_call(eng, stats);
+    }
+    if ((rc = finish_call(eng, stats))) return rc;
     for (size_t ps = 0; ps < eng->last_passes; ++ps) {
       const size_t s0 = ps * PW, np = std::min(PW, S - s0);
       if (eng->h_ctl[ps].narrow) {
@@ -1131,6 +1186,8 @@ int msbfs_engine_create(int device, int method, msbfs_engine** out) {
   e->zero_copy = !(zc && zc[0] == '0');
   const char* nr = getenv("MSBFS_NARROW");
   e->narrow = !(nr && nr[0] == '0');
+  const char* sr = getenv("MSBFS_SPLIT_ROWS");
+  if (sr) e->split_frac = std::min(1.0, std::max(0.0, atof(sr)));
   *out = eng.release();
   return MSBFS_OK;
 }
@@ -1146,6 +1203,7 @@ void msbfs_engine_destroy(msbfs_engine* e) {
   cudaFree(e->d_dist8);
   if (e->h_dist8) cudaFreeHost(e->h_dist8);
   for (cudaEvent_t ev : e->chunk_events) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : e->split_events) cudaEventDestroy(ev);
   cudaFree(e->d_reach);
   cudaFree(e->d_cta_queue);
   cudaFree(e->d_cta_bits);

@@ -1270,7 +1270,8 @@ __global__ void __launch_bounds__(RED_BLOCK, RED_MIN_BLOCKS) reduce_kernel(Level
 // (vertex tile, word group) items; see MatGeo for the tile. Passes that want
 // per-source reductions run reduce_kernel instead.
 template <int W>
-__global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(LevelParams p) {
+__global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS)
+    materialize_kernel(LevelParams p, uint32_t phase) {
   using G = MatGeo<W>;
   extern __shared__ uint32_t mat_sh[];  // [1 + NP][TW][RS]: visited words, then planes
   const PassDesc* dsc = p.desc;
@@ -1283,16 +1284,24 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(
   // Byte rows when the pass asks for them and every distance fits a byte
   // (0xFF is kept for unreachable); the control block tells the host.
   const bool narrow = dsc->dist8 && !dsc->reach && dmax < 255u;
-  if (narrow && blockIdx.x == 0 && threadIdx.x == 0) p.ctl->narrow = 1;
+  if (phase == MAT_BYTES && !narrow) return;
+  // Word columns this launch writes, whether as bytes, and whether it
+  // clears the state it read (the last launch over the pass does).
+  const uint32_t wsplit = min(dsc->row_split / 32, Wu);
+  const uint32_t wlo = phase == MAT_BYTES ? wsplit : 0u;
+  const uint32_t whi = (phase == MAT_WIDE && narrow) ? wsplit : Wu;
+  const bool bytes = phase == MAT_BYTES || (phase == MAT_ALL && narrow);
+  const bool clear = phase != MAT_BYTES;
+  if (bytes && blockIdx.x == 0 && threadIdx.x == 0) p.ctl->narrow = 1;
   const MatOut out{dsc->dist, dsc->reach, dsc->reach_wpv, dsc->reach_col,
-                   narrow ? dsc->dist8 : nullptr};
+                   bytes ? dsc->dist8 : nullptr};
   const uint32_t V = p.V;
   const size_t VW = (size_t)V * W;
   const uint32_t tid = threadIdx.x;
   const uint32_t lane = tid & 31;
   const uint32_t warp = tid >> 5;
-  const bool vec_ok = narrow ? (V % 2 == 0) && (((uintptr_t)out.dist8 & 1) == 0)
-                             : (V % 2 == 0) && (((uintptr_t)out.dist & 7) == 0);
+  const bool vec_ok = bytes ? (V % 2 == 0) && (((uintptr_t)out.dist8 & 1) == 0)
+                            : (V % 2 == 0) && (((uintptr_t)out.dist & 7) == 0);
   const uint32_t ngu = (Wu + G::TW - 1) / G::TW;  // word groups in use
   const size_t nitems = (size_t)((V + G::TV - 1) / G::TV) * ngu;
   const uint32_t o = 4 * tid;  // tile word offset of this thread's four words
@@ -1320,13 +1329,14 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(
       if (inb && (a == 0 || vec_planes)) {
         const uint4 t = *reinterpret_cast<const uint4*>(src + gw);
         x[0] = t.x; x[1] = t.y; x[2] = t.z; x[3] = t.w;
-        if (t.x | t.y | t.z | t.w) *reinterpret_cast<uint4*>(src + gw) = make_uint4(0, 0, 0, 0);
+        if (clear && (t.x | t.y | t.z | t.w))
+          *reinterpret_cast<uint4*>(src + gw) = make_uint4(0, 0, 0, 0);
       } else if constexpr (W <= 16) {
 #pragma unroll
         for (int k = 0; k < 4; ++k)
           if (gw + k < VW) {
             x[k] = src[gw + k];
-            if (x[k]) src[gw + k] = 0;
+            if (clear && x[k]) src[gw + k] = 0;
           }
       }
       uint32_t* dst = mat_sh + a * G::ARR;
@@ -1335,7 +1345,8 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS) materialize_kernel(
     }
     __syncthreads();
     for (uint32_t cs = warp; cs < MAT_COLS; cs += MAT_BLOCK / 32) {
-      if (g * G::TW + cs % G::TW >= Wu) continue;  // no sources in this word
+      const uint32_t cw = g * G::TW + cs % G::TW;
+      if (cw < wlo || cw >= whi) continue;  // no sources of this launch in this word
       switch (npu) {
 #define MAT_CASE(n) \
   case n: mat_column<W, n>(p, out, mat_sh, v0, g, cs, lane, P, use_ovf, vec_ok); break;
@@ -1484,22 +1495,22 @@ void launch_level(const LevelParams& p, const LevelKernelInfo& k, uint32_t dir, 
 
 template <int W>
 static void launch_mat_t(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
-                         cudaStream_t s) {
+                         cudaStream_t s, uint32_t phase) {
   if (reduce)
     reduce_kernel<W><<<k.red_grid, k.red_block, 0, s>>>(p);
   else
-    materialize_kernel<W><<<k.mat_grid, k.mat_block, k.mat_smem, s>>>(p);
+    materialize_kernel<W><<<k.mat_grid, k.mat_block, k.mat_smem, s>>>(p, phase);
 }
 void launch_materialize(const LevelParams& p, const LevelKernelInfo& k, bool reduce,
-                        cudaStream_t s) {
+                        cudaStream_t s, uint32_t phase) {
   switch (p.W) {
-    case 1: launch_mat_t<1>(p, k, reduce, s); break;
-    case 2: launch_mat_t<2>(p, k, reduce, s); break;
-    case 4: launch_mat_t<4>(p, k, reduce, s); break;
-    case 8: launch_mat_t<8>(p, k, reduce, s); break;
-    case 16: launch_mat_t<16>(p, k, reduce, s); break;
-    case 32: launch_mat_t<32>(p, k, reduce, s); break;
-    case 64: launch_mat_t<64>(p, k, reduce, s); break;
+    case 1: launch_mat_t<1>(p, k, reduce, s, phase); break;
+    case 2: launch_mat_t<2>(p, k, reduce, s, phase); break;
+    case 4: launch_mat_t<4>(p, k, reduce, s, phase); break;
+    case 8: launch_mat_t<8>(p, k, reduce, s, phase); break;
+    case 16: launch_mat_t<16>(p, k, reduce, s, phase); break;
+    case 32: launch_mat_t<32>(p, k, reduce, s, phase); break;
+    case 64: launch_mat_t<64>(p, k, reduce, s, phase); break;
   }
 }
 
