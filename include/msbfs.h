@@ -163,7 +163,8 @@ int msbfs_engine_set_tuning(msbfs_engine *engine, uint32_t max_words_per_pass,
  * times the call on the given sources (per-source statistics output, CUDA
  * events) while it varies one setting at a time over its candidates -- words
  * per vertex of a pass, alpha, beta, the in-edge slice length of bottom-up
- * steps and the frontier-bitmap threshold -- keeping a change only when it is
+ * steps, the frontier-bitmap threshold and the in-degree from which a whole
+ * warp scans a vertex -- keeping a change only when it is
  * faster, then applies the best settings to the engine (and the slice length
  * to the graph). With a cache path, a class already in the file is applied
  * without timing and new classes are appended. Results never depend on the
@@ -175,6 +176,7 @@ typedef struct msbfs_tuning {
   uint32_t beta;               /* bottom-up -> top-down: frontier vertices * beta < V  */
   uint32_t hub_split;          /* in-edge slice length of bottom-up steps              */
   uint32_t bitmap_div;         /* frontier-bitmap test below V / bitmap_div vertices    */
+  uint32_t warp_scan_degree;   /* in-degree from which a whole warp scans a vertex      */
   uint32_t from_cache;         /* 1: read from the cache file, not timed               */
   uint32_t trials;             /* settings timed                                        */
   uint32_t level_path;         /* 0: the call runs on the CTA path, nothing tuned       */

@@ -46,7 +46,8 @@ STRUCTS = {
         ("max_rows", "max_rows"), ("max_cols", "max_cols"), ("message", "message")]),
     "msbfs_tuning": ("Tuning", [
         ("max_words_per_pass", "max_words_per_pass"), ("alpha", "alpha"), ("beta", "beta"),
-        ("hub_split", "hub_split"), ("bitmap_div", "bitmap_div"), ("from_cache", "from_cache"),
+        ("hub_split", "hub_split"), ("bitmap_div", "bitmap_div"),
+        ("warp_scan_degree", "warp_scan_degree"), ("from_cache", "from_cache"),
         ("trials", "trials"), ("level_path", "level_path"), ("ms", "ms"),
         ("default_ms", "default_ms"), ("class_name", "class_name")]),
     "msbfs_batch_graph": ("BatchGraph", [

@@ -359,9 +359,9 @@ def test_autotune_same_bytes_and_cache(native, oracle, tmp_path):
     try:
         t2 = eng.autotune(g, src, cache_path=cache)
         assert t2["from_cache"] and t2["trials"] == 0
-        assert {k: t2[k] for k in ("max_words_per_pass", "alpha", "beta", "hub_split",
-                                   "bitmap_div")} == \
-            {k: t[k] for k in ("max_words_per_pass", "alpha", "beta", "hub_split", "bitmap_div")}
+        keys = ("max_words_per_pass", "alpha", "beta", "hub_split", "bitmap_div",
+                "warp_scan_degree")
+        assert {k: t2[k] for k in keys} == {k: t[k] for k in keys}
         assert_same(eng.run_ms_bfs(g, src), want, g, src, "settings from the cache")
         road = native.wilson_grid(50, 50, 40, 2)
         rs = native.sample_sources(road, 40, 1)

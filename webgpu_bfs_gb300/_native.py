@@ -111,6 +111,7 @@ class Tuning(C.Structure):
         ("beta", C.c_uint32),
         ("hub_split", C.c_uint32),
         ("bitmap_div", C.c_uint32),
+        ("warp_scan_degree", C.c_uint32),
         ("from_cache", C.c_uint32),
         ("trials", C.c_uint32),
         ("level_path", C.c_uint32),

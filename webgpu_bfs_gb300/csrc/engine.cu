@@ -1494,13 +1494,14 @@ namespace {
 
 // Settings of the level-synchronous path that the autotuner varies.
 struct LevelSettings {
-  uint32_t words, alpha, beta, split, bits_div;
+  uint32_t words, alpha, beta, split, bits_div, heavy;
   uint32_t& at(int i) {
-    return i == 0 ? words : i == 1 ? alpha : i == 2 ? beta : i == 3 ? split : bits_div;
+    return i == 0 ? words : i == 1 ? alpha : i == 2 ? beta : i == 3 ? split : i == 4 ? bits_div
+                                                                                  : heavy;
   }
   bool operator==(const LevelSettings& o) const {
     return words == o.words && alpha == o.alpha && beta == o.beta && split == o.split &&
-           bits_div == o.bits_div;
+           bits_div == o.bits_div && heavy == o.heavy;
   }
 };
 
@@ -1515,6 +1516,7 @@ int apply_settings(msbfs_engine* eng, msbfs_graph* g, const LevelSettings& s) {
   eng->alpha = s.alpha;
   eng->beta = s.beta;
   eng->bits_div = s.bits_div;
+  eng->heavy = s.heavy;
   if (s.split != g->split) return build_bottom_up_tables(eng, g, s.split);
   return MSBFS_OK;
 }
@@ -1555,7 +1557,7 @@ extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint
       msbfs::graph_class(g->V, g->E, g->max_deg) + "/s" + std::to_string(bucket);
   msbfs_tuning t{};
   std::strncpy(t.class_name, key.c_str(), sizeof t.class_name - 1);
-  LevelSettings best{e->max_words, e->alpha, e->beta, g->split, e->bits_div};
+  LevelSettings best{e->max_words, e->alpha, e->beta, g->split, e->bits_div, e->heavy};
   auto report = [&](const LevelSettings& s) {
     // The words a pass of this call uses (a cap above the sources' need
     // makes no difference).
@@ -1566,6 +1568,7 @@ extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint
     t.beta = s.beta;
     t.hub_split = s.split;
     t.bitmap_div = s.bits_div;
+    t.warp_scan_degree = s.heavy;
     if (out) *out = t;
     return MSBFS_OK;
   };
@@ -1573,13 +1576,14 @@ extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint
   if (method_path(method) == MSBFS_PATH_CTA) return report(best);
   t.level_path = 1;
   const bool shared = !g->users.empty() || g->eng != e;  // other engines hold its tables
-  // Cache: one line per class, "class words alpha beta split bitmap_div ms".
+  // Cache: one line per class,
+  // "class words alpha beta split bitmap_div warp_scan_degree ms".
   if (cache_path) {
     std::ifstream in(cache_path);
     std::string k;
     LevelSettings s{};
     double ms = 0;
-    while (in >> k >> s.words >> s.alpha >> s.beta >> s.split >> s.bits_div >> ms) {
+    while (in >> k >> s.words >> s.alpha >> s.beta >> s.split >> s.bits_div >> s.heavy >> ms) {
       if (k != key) continue;
       if (shared) s.split = g->split;
       if ((rc = apply_settings(e, g, s))) return rc;
@@ -1599,10 +1603,11 @@ extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint
       {4, 8, 14, 28, 56},                                      // alpha
       {6, 12, 24, 64, 256},                                    // beta
       {256, 512, 1024},                                        // slice length
-      {16, 64, 256}};                                          // bitmap divisor
+      {16, 64, 256},                                           // bitmap divisor
+      {8, 16, 32, 64}};                                        // warp-scan in-degree
   // One setting at a time, each from the best found so far; a change is
   // kept only when it is at least 2% faster (timing noise).
-  for (int i = 0; i < 5; ++i) {
+  for (int i = 0; i < 6; ++i) {
     if (i == 3 && shared) continue;
     const LevelSettings base = best;
     for (uint32_t c : cands[i]) {
@@ -1624,7 +1629,7 @@ extern "C" int msbfs_engine_autotune(msbfs_engine* e, msbfs_graph* g, const uint
   if (cache_path) {
     std::ofstream o(cache_path, std::ios::app);
     o << key << ' ' << best.words << ' ' << best.alpha << ' ' << best.beta << ' ' << best.split
-      << ' ' << best.bits_div << ' ' << best_ms << '\n';
+      << ' ' << best.bits_div << ' ' << best.heavy << ' ' << best_ms << '\n';
   }
   return report(best);
 }

@@ -75,6 +75,7 @@ pub struct MsbfsTuning {
     pub beta: u32,
     pub hub_split: u32,
     pub bitmap_div: u32,
+    pub warp_scan_degree: u32,
     pub from_cache: u32,
     pub trials: u32,
     pub level_path: u32,
@@ -91,6 +92,7 @@ impl Default for MsbfsTuning {
             beta: 0,
             hub_split: 0,
             bitmap_div: 0,
+            warp_scan_degree: 0,
             from_cache: 0,
             trials: 0,
             level_path: 0,
