@@ -421,9 +421,12 @@ def run_ours(args, spec):
     tedges = eng.traversed_edges_device(g, out.data_ptr(), S)
     gteps = tedges * args.steps / (max_ms / 1000.0) / 1e9 * world
 
-    # per pass: init, one level kernel per level, materialise, cleanup; the
-    # CTA path is one launch
-    launches_per_step = (st["levels"] + 3) * st["passes"] if st["path"] != 4 else 1
+    # per pass: init, per level the bottom-up and the top-down kernel (the one
+    # whose direction is not current returns at once; push- or pull-only
+    # methods have one), materialise, cleanup; the CTA path is one launch
+    per_level = 2 if st["path"] == 3 else 1
+    launches_per_step = ((per_level * st["levels"] + 3) * st["passes"] if st["path"] != 4
+                         else 1)
 
     # ---- roofline of the level kernel: per-launch CUDA events in a host-driven
     # replay of the same step, algorithmic bytes from the kernel's own counters
