@@ -500,8 +500,10 @@ int msbfs_sample_sources(const msbfs_csr *csr, size_t count, uint64_t seed,
  * pulls (graph, source range) items from a device work list. Per graph class
  * (road-like / mesh / power-law x vertex-count bucket) the autotuner times
  * candidate configurations (block-synchronous bit-parallel BFS with 1-8
- * words per vertex and three bottom-up thresholds, or one single-source BFS
- * per source with 1/4/16 sources per item) on sample graphs of that class
+ * words per vertex, three bottom-up thresholds and two tile shapes -- a
+ * thread per vertex word, or a thread per vertex holding all its words --
+ * or one single-source BFS per source with 1/4/16 sources per item) on
+ * sample graphs of that class
  * and caches the fastest, optionally in a text file. Results (S*V u32 per
  * graph, same bytes as msbfs_run_ms_bfs) stay in device memory until read. */
 #define MSBFS_BATCH_MAX_VERTICES 262144u
@@ -528,8 +530,9 @@ int msbfs_batch_run_per_graph(msbfs_batch *batch, const msbfs_batch_graph *graph
 /* Copies graph i's S*V distance rows to host memory. */
 int msbfs_batch_result(msbfs_batch *batch, size_t graph_index, uint32_t *out);
 /* The tuned configuration of graph i's class: alg 0 = bit-parallel block
- * (words = max words per vertex, param = bottom-up divisor), 1 = one source
- * per BFS (param = sources per item). */
+ * with a thread per vertex word, 2 = the same with a thread per vertex
+ * (words = max words per vertex, param = bottom-up divisor for both),
+ * 1 = one source per BFS (param = sources per item). */
 int msbfs_batch_config(const msbfs_batch *batch, size_t graph_index, uint32_t *alg,
                        uint32_t *words, uint32_t *param, char *class_name,
                        size_t class_len);

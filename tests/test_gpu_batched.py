@@ -73,3 +73,33 @@ def test_batched_untuned_and_rerun(native, oracle, alg_case):
                 assert_same(b.result(i), want, g, s, f"{alg_case} {i}")
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("div", [2, 1024])
+def test_batched_vertex_tiles_match_oracle(native, oracle, tmp_path, div):
+    """The vertex-tile shape (a thread per vertex holding all its words),
+    forced for every class through the autotuner's cache file, with a
+    bottom-up threshold that makes nearly every level bottom-up (div 2 is
+    for graphs whose frontier exceeds V/2; 1024 sends almost every level
+    bottom-up) -- rows equal the oracle's at 2, 4 and 8 words per vertex."""
+    items = _mixed_batch(native, n_er=6, n_grid=3, n_rmat=3, seed=9)
+    b = native.BatchedBfs(items)
+    try:
+        classes = sorted({b.config(i)["class"] for i in range(len(items))})
+    finally:
+        b.close()
+    for words in (2, 4, 8):
+        cache = tmp_path / f"vertex_tiles_{words}_{div}.txt"
+        # "class alg wcap div chunk shape ms": bit-parallel, vertex tiles
+        cache.write_text("".join(f"{c} 0 {words} {div} 4 1 1.0\n" for c in classes))
+        b = native.BatchedBfs(items)
+        try:
+            b.autotune(samples_per_class=1, cache_path=str(cache))
+            assert all(b.config(i)["alg"] == "bit_parallel_vertex_tiles"
+                       for i in range(len(items)))
+            b.run()
+            for i, (g, s) in enumerate(items):
+                want = oracle.ms_bfs_fifo(g.num_vertices, g.row_offsets, g.col_indices, s)
+                assert_same(b.result(i), want, g, s, f"vertex tiles W<={words} div={div} {i}")
+        finally:
+            b.close()

@@ -629,7 +629,7 @@ class BatchedBfs:
     persistent launch (msbfs_batch_*). ``items`` is a sequence of
     ``(CsrGraph, sources)``. Results stay on the device until ``result(i)``."""
 
-    ALG_NAMES = {0: "bit_parallel_block", 1: "source_per_bfs"}
+    ALG_NAMES = {0: "bit_parallel_block", 1: "source_per_bfs", 2: "bit_parallel_vertex_tiles"}
 
     def __init__(self, items, device: int = 0):
         self._keep = []

@@ -40,6 +40,7 @@
 namespace msbfs {
 
 enum : uint32_t { ALG_BP = 0, ALG_CTA = 1 };
+enum : uint32_t { SHAPE_WORD = 0, SHAPE_VERTEX = 1 };
 constexpr int BATCH_BLOCK = 512;
 constexpr uint32_t BATCH_DIST_MAX = 0xffffffffu;
 
@@ -48,6 +49,9 @@ struct BatchGraph {
   uint32_t alg;    // ALG_*
   uint32_t W;      // words per vertex (ALG_BP), power of two <= 8
   uint32_t div;    // ALG_BP: bottom-up when the frontier holds > V / div vertices
+  uint32_t shape;  // ALG_BP tile shape: SHAPE_WORD (a thread per vertex word, a warp
+                   // covers 32/W vertices x W words) or SHAPE_VERTEX (a thread per
+                   // vertex with all W words, each edge list read once)
   const uint32_t* off;   // CSR
   const uint32_t* idx;
   const uint32_t* coff;  // CSC (aliases the CSR when symmetric)
@@ -82,6 +86,7 @@ __device__ __forceinline__ uint32_t bword_mask(uint32_t P, uint32_t k) {
 
 // Block-synchronous bit-parallel BFS of sources [s0, s0+P) of graph g.
 // Scratch: vis[V*W], Fa[V*W], Fb[V*W], Qa[V], Qb[V]; sbits: V bits (shared).
+template <bool VT>
 __device__ void bp_item(const BatchGraph& g, uint32_t s0, uint32_t P, uint32_t* scr,
                         uint32_t* sbits, uint32_t* s_cnt) {
   const uint32_t V = g.V, W = g.W, lw = __ffs(W) - 1;
@@ -115,7 +120,49 @@ __device__ void bp_item(const BatchGraph& g, uint32_t s0, uint32_t P, uint32_t* 
   __syncthreads();
   for (uint32_t L = 0; qa > 0 && L <= V; ++L) {
     const uint32_t d = L + 1;
-    if ((size_t)qa * g.div > V) {
+    if (VT && (size_t)qa * g.div > V && g.shape == SHAPE_VERTEX) {
+      // bottom-up, a thread per vertex: its in-edge list is read once for
+      // all W words and the scan stops once every needed lane is covered.
+      for (uint32_t v = tid; v < V; v += bs) {
+        uint32_t needed[8], cand[8];
+        uint32_t any = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+          needed[k] = k < W ? ~vis[(v << lw) + k] & bword_mask(P, k) : 0u;
+          cand[k] = 0;
+          any |= needed[k];
+        }
+        if (!any) continue;
+        for (uint32_t e = g.coff[v]; e < g.coff[v + 1]; ++e) {
+          const uint32_t* fu = Fa + (g.cidx[e] << lw);
+          uint32_t left = 0;
+#pragma unroll
+          for (uint32_t k = 0; k < 8; ++k) {
+            if (k < W) cand[k] |= fu[k];
+            left |= needed[k] & ~cand[k];
+          }
+          if (!left) break;
+        }
+        bool found = false;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+          uint32_t newly = cand[k] & needed[k];
+          if (!newly) continue;
+          found = true;
+          vis[(v << lw) + k] |= newly;
+          Fb[(v << lw) + k] = newly;
+          while (newly) {
+            const uint32_t b = __ffs(newly) - 1;
+            newly &= newly - 1;
+            g.dist[(size_t)(s0 + k * 32 + b) * V + v] = d;
+          }
+        }
+        if (found) {
+          const uint32_t vb = 1u << (v & 31);
+          if (!(atomicOr(&sbits[v >> 5], vb) & vb)) Qb[atomicAdd(&s_cnt[1], 1u)] = v;
+        }
+      }
+    } else if ((size_t)qa * g.div > V) {
       // bottom-up: thread per (vertex, word); the owner updates its word.
       for (uint32_t i = tid; i < VW; i += bs) {
         const uint32_t v = i >> lw, k = i & (W - 1);
@@ -137,6 +184,44 @@ __device__ void bp_item(const BatchGraph& g, uint32_t s0, uint32_t P, uint32_t* 
         }
         const uint32_t vb = 1u << (v & 31);
         if (!(atomicOr(&sbits[v >> 5], vb) & vb)) Qb[atomicAdd(&s_cnt[1], 1u)] = v;
+      }
+    } else if (VT && g.shape == SHAPE_VERTEX) {
+      // top-down, a thread per frontier vertex: each out-edge's target is
+      // read once for all W words.
+      for (uint32_t i = tid; i < qa; i += bs) {
+        const uint32_t u = Qa[i];
+        uint32_t f[8];
+        uint32_t any = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+          f[k] = k < W ? Fa[(u << lw) + k] : 0u;
+          any |= f[k];
+        }
+        if (!any) continue;
+        for (uint32_t e = g.off[u]; e < g.off[u + 1]; ++e) {
+          const uint32_t v = g.idx[e];
+          bool found = false;
+#pragma unroll
+          for (uint32_t k = 0; k < 8; ++k) {
+            if (!f[k]) continue;
+            uint32_t* vw = &vis[(v << lw) + k];
+            const uint32_t needed = f[k] & ~__ldcg(vw);
+            if (!needed) continue;
+            uint32_t newly = needed & ~atomicOr(vw, needed);
+            if (!newly) continue;
+            found = true;
+            atomicOr(&Fb[(v << lw) + k], newly);
+            while (newly) {
+              const uint32_t b = __ffs(newly) - 1;
+              newly &= newly - 1;
+              g.dist[(size_t)(s0 + k * 32 + b) * V + v] = d;
+            }
+          }
+          if (found) {
+            const uint32_t vb = 1u << (v & 31);
+            if (!(atomicOr(&sbits[v >> 5], vb) & vb)) Qb[atomicAdd(&s_cnt[1], 1u)] = v;
+          }
+        }
       }
     } else {
       // top-down: thread per (frontier vertex, word).
@@ -233,6 +318,10 @@ __device__ void cta_item(const BatchGraph& g, uint32_t s0, uint32_t n, uint32_t*
   }
 }
 
+// VT = true compiles the vertex-tile branches in as well; their per-thread
+// word arrays double the kernel's registers (and halve its occupancy), so
+// a launch takes that form only when some graph's class runs vertex tiles.
+template <bool VT>
 __global__ void __launch_bounds__(BATCH_BLOCK) batch_kernel(BatchParams p) {
   extern __shared__ uint32_t sbits[];
   __shared__ uint32_t s_item;
@@ -249,7 +338,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) batch_kernel(BatchParams p) {
     if (g.alg == ALG_CTA)
       cta_item(g, item.s0, item.n, scr, sbits, s_cnt);
     else
-      bp_item(g, item.s0, item.n, scr, sbits, s_cnt);
+      bp_item<VT>(g, item.s0, item.n, scr, sbits, s_cnt);
   }
 }
 
@@ -266,6 +355,7 @@ struct ClassConfig {
   uint32_t wcap = 8;   // ALG_BP: max words per vertex per item
   uint32_t div = 16;   // ALG_BP: bottom-up threshold
   uint32_t chunk = 4;  // ALG_CTA: sources per item
+  uint32_t shape = SHAPE_WORD;  // ALG_BP: tile shape
   double ms = 0;       // tuning time of the winner
 };
 
@@ -308,7 +398,8 @@ struct msbfs_batch {
   size_t d_items_cap = 0;
   uint32_t* d_scratch = nullptr;
   size_t scratch_words = 0;
-  int grid = 0;
+  int grid = 0;     // resident blocks of the word-tile kernel
+  int grid_vt = 0;  // and of the kernel with vertex tiles compiled in
   size_t smem = 0;
   size_t max_V = 0;
   msbfs_engine* eng = nullptr;  // plain per-graph comparison path
@@ -334,6 +425,7 @@ void make_items(const msbfs_batch* b, uint32_t gi, const ClassConfig& c, BatchGr
   const HostGraphInfo& h = b->info[gi];
   g.alg = c.alg;
   g.div = c.div;
+  g.shape = c.shape;
   if (c.alg == ALG_CTA) {
     g.W = 1;
     for (uint32_t s0 = 0; s0 < g.S; s0 += c.chunk) {
@@ -359,12 +451,14 @@ int launch_batch(msbfs_batch* b, const std::vector<uint32_t>& subset, float* ms_
   std::vector<BatchItem> items;
   std::vector<double> cost;
   std::vector<BatchGraph> gs = b->graphs;
+  bool vt = false;
   const size_t n = subset.empty() ? b->graphs.size() : subset.size();
   for (size_t j = 0; j < n; ++j) {
     const uint32_t gi = subset.empty() ? (uint32_t)j : subset[j];
     auto it = b->configs.find(b->info[gi].cls);
     const ClassConfig c = it != b->configs.end() ? it->second : ClassConfig{};
     make_items(b, gi, c, gs[gi], items, cost);
+    vt |= gs[gi].alg == ALG_BP && gs[gi].shape == SHAPE_VERTEX;
   }
   // Longest items first (LPT) so the tail of the launch is short.
   std::vector<size_t> ord(items.size());
@@ -392,8 +486,12 @@ int launch_batch(msbfs_batch* b, const std::vector<uint32_t>& subset, float* ms_
   p.scratch = b->d_scratch;
   p.scratch_words = b->scratch_words;
   BCK(cudaEventRecord(b->ev0, b->stream));
-  const int grid = (int)std::min<size_t>((size_t)b->grid, std::max<size_t>(sorted.size(), 1));
-  batch_kernel<<<grid, BATCH_BLOCK, b->smem, b->stream>>>(p);
+  const int grid = (int)std::min<size_t>((size_t)(vt ? b->grid_vt : b->grid),
+                                         std::max<size_t>(sorted.size(), 1));
+  if (vt)
+    batch_kernel<true><<<grid, BATCH_BLOCK, b->smem, b->stream>>>(p);
+  else
+    batch_kernel<false><<<grid, BATCH_BLOCK, b->smem, b->stream>>>(p);
   BCK(cudaGetLastError());
   BCK(cudaEventRecord(b->ev1, b->stream));
   BCK(cudaEventSynchronize(b->ev1));
@@ -480,16 +578,20 @@ int msbfs_batch_create(int device, const msbfs_batch_graph* graphs, size_t n, ms
   // ALG_CTA (2V) for the largest graph.
   b->scratch_words = 3 * maxVW * 8 + 2 * maxVW + 64;
   b->smem = ((b->max_V + 31) / 32) * 4;
-  BCK(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  BCK(cudaFuncSetAttribute(batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)std::max<size_t>(b->smem, 4)));
-  int occ = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, BATCH_BLOCK, b->smem);
+  BCK(cudaFuncSetAttribute(batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)std::max<size_t>(b->smem, 4)));
+  int occ = 0, occ_vt = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<false>, BATCH_BLOCK, b->smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_vt, batch_kernel<true>, BATCH_BLOCK, b->smem);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   b->grid = std::max(1, occ) * sms;
   // Scratch is per resident block; keep it within 8 GiB by running fewer
   // blocks when the largest graph is big.
   const size_t per_block = b->scratch_words * 4;
   b->grid = (int)std::max<size_t>(1, std::min<size_t>(b->grid, (size_t(8) << 30) / per_block));
+  b->grid_vt = std::min(b->grid, std::max(1, occ_vt) * sms);
   BCK(cudaMalloc((void**)&b->d_scratch, (size_t)b->grid * per_block));
   *out = b.release();
   return MSBFS_OK;
@@ -505,25 +607,28 @@ void msbfs_batch_destroy(msbfs_batch* b) {
 int msbfs_batch_autotune(msbfs_batch* b, size_t samples_per_class, const char* cache_path) {
   if (!b) return MSBFS_ERR_INVALID_ARGUMENT;
   BCK(cudaSetDevice(b->device));
-  // Cached choices first: "class alg wcap div chunk ms" per line.
+  // Cached choices first: "class alg wcap div chunk shape ms" per line.
   std::map<std::string, ClassConfig> cached;
   if (cache_path) {
     std::ifstream in(cache_path);
     std::string cls;
     ClassConfig c;
-    while (in >> cls >> c.alg >> c.wcap >> c.div >> c.chunk >> c.ms) cached[cls] = c;
+    while (in >> cls >> c.alg >> c.wcap >> c.div >> c.chunk >> c.shape >> c.ms) cached[cls] = c;
   }
   std::map<std::string, std::vector<uint32_t>> members;
   for (uint32_t i = 0; i < b->info.size(); ++i) members[b->info[i].cls].push_back(i);
   std::vector<ClassConfig> cands;
   for (uint32_t w : {1u, 2u, 4u, 8u})
-    for (uint32_t dv : {4u, 16u, 64u}) {
-      ClassConfig c;
-      c.alg = ALG_BP;
-      c.wcap = w;
-      c.div = dv;
-      cands.push_back(c);
-    }
+    for (uint32_t dv : {4u, 16u, 64u})
+      for (uint32_t sh : {(uint32_t)SHAPE_WORD, (uint32_t)SHAPE_VERTEX}) {
+        if (w == 1 && sh == SHAPE_VERTEX) continue;  // one word: the two shapes coincide
+        ClassConfig c;
+        c.alg = ALG_BP;
+        c.wcap = w;
+        c.div = dv;
+        c.shape = sh;
+        cands.push_back(c);
+      }
   for (uint32_t ch : {1u, 4u, 16u}) {
     ClassConfig c;
     c.alg = ALG_CTA;
@@ -562,7 +667,7 @@ int msbfs_batch_autotune(msbfs_batch* b, size_t samples_per_class, const char* c
     std::ofstream o(cache_path);
     for (auto& kv : cached)
       o << kv.first << " " << kv.second.alg << " " << kv.second.wcap << " " << kv.second.div
-        << " " << kv.second.chunk << " " << kv.second.ms << "\n";
+        << " " << kv.second.chunk << " " << kv.second.shape << " " << kv.second.ms << "\n";
   }
   return MSBFS_OK;
 }
@@ -624,7 +729,7 @@ int msbfs_batch_config(const msbfs_batch* b, size_t i, uint32_t* alg, uint32_t* 
   const std::string& cls = b->info[i].cls;
   auto it = b->configs.find(cls);
   const ClassConfig c = it != b->configs.end() ? it->second : ClassConfig{};
-  if (alg) *alg = c.alg;
+  if (alg) *alg = (c.alg == ALG_BP && c.shape == SHAPE_VERTEX) ? 2u : c.alg;
   if (words) *words = c.wcap;
   if (param) *param = c.alg == ALG_CTA ? c.chunk : c.div;
   if (class_name && class_len) {
