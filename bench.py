@@ -492,12 +492,13 @@ def run_ours(args, spec):
         # e2e calls, which then overwrite the buffer with their rows).
         dev = torch.zeros(S * V, dtype=torch.int32, device="cuda")
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        for _ in range(2):
+        link_ms = float("inf")
+        for _ in range(4):  # the first copy warms the buffer; best of the rest
             e0.record()
             host_out.copy_(dev, non_blocking=True)
             e1.record()
             torch.cuda.synchronize()
-        link_ms = e0.elapsed_time(e1)
+            link_ms = min(link_ms, e0.elapsed_time(e1))
         del dev
         host_src = torch.from_numpy(src.astype(np.int32)).pin_memory()
         hs = host_src.numpy().view(np.uint32)

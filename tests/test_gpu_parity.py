@@ -414,3 +414,45 @@ def test_byte_row_transport_mixed_passes(native, oracle, monkeypatch, pinned):
         assert_same(out, want, g, src, f"narrow={narrow} pinned={pinned}")
         outs[narrow] = out
     assert np.array_equal(outs["1"], outs["0"])
+
+
+@pytest.mark.parametrize("depth", [7, 8, 127, 128, 200, 254, 255, 256])
+def test_materialisation_depth_boundaries(native, oracle, monkeypatch, depth):
+    """Distances come out of the level planes by a bit-matrix transpose when
+    every distance is below 255 (sign-replicating byte selects up to 7 planes,
+    a compare at 8) and by per-plane bit extraction otherwise. An R-MAT
+    component beside a path of depth + 1 vertices (odd and even vertex
+    counts), sources including the path's end so the deepest distance is
+    `depth`: u32 rows (never narrowed), byte rows widened on the host, and
+    page-locked output, at one and at several words per vertex, all equal
+    the oracle's."""
+    torch = pytest.importorskip("torch")
+    r = native.generate_graph500_rmat(10, 8, 23)
+    n0 = r.num_vertices
+    edges = [(u, int(v)) for u in range(n0) for v in r.neighbors(u)]
+    edges += [(n0 + i, n0 + i + 1) for i in range(depth)]
+    edges += [(n0 + i + 1, n0 + i) for i in range(depth)]
+    g = native.CsrGraph.from_edge_list(n0 + depth + 1, edges)
+    deg = np.diff(r.row_offsets.astype(np.int64))
+    live = np.flatnonzero(deg > 0).astype(np.uint32)
+    src = np.concatenate([live[:37], np.array([n0 + depth, n0 + depth // 2, n0], np.uint32)])
+    want = _oracle(oracle, g, src)
+    for narrow, pinned in (("0", False), ("1", False), ("1", True)):
+        monkeypatch.setenv("MSBFS_NARROW", narrow)
+        for words in (1, 16):
+            eng = native.GpuBfsEngine(native.GpuBfsMethod.PushPullAdaptive)
+            try:
+                eng.set_tuning(max_words_per_pass=words)
+                if pinned:
+                    buf = torch.empty(src.size * g.num_vertices, dtype=torch.int32,
+                                      pin_memory=True)
+                    out = buf.numpy().view(np.uint32)
+                    out[:] = 7
+                    eng.run_ms_bfs_into(g, src, out)
+                    out = out.copy()
+                else:
+                    out = eng.run_ms_bfs(g, src)
+                assert eng.last_stats["levels"] >= depth
+            finally:
+                eng.close()
+            assert_same(out, want, g, src, f"depth={depth} narrow={narrow} pinned={pinned} W={words}")

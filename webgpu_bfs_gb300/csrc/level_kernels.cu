@@ -1033,17 +1033,90 @@ struct MatOut {
   uint8_t* dist8;  // non-null: rows as one byte per distance (all below 255)
 };
 
+// Byte transpose of four words: byte i of r[m] is byte m of a[i].
+__device__ __forceinline__ void byte_transpose4(uint32_t a0, uint32_t a1, uint32_t a2,
+                                                uint32_t a3, uint32_t* r) {
+  const uint32_t t0 = __byte_perm(a0, a1, 0x5140), t1 = __byte_perm(a0, a1, 0x7362);
+  const uint32_t t2 = __byte_perm(a2, a3, 0x5140), t3 = __byte_perm(a2, a3, 0x7362);
+  r[0] = __byte_perm(t0, t2, 0x5410);
+  r[1] = __byte_perm(t0, t2, 0x7632);
+  r[2] = __byte_perm(t1, t3, 0x5410);
+  r[3] = __byte_perm(t1, t3, 0x7632);
+}
+
+// Transposes the 8x8 bit matrix held in (lo, hi), row r in byte r and column
+// c in bit c of each byte, by three exchanges of 1x1, 2x2 and 4x4 blocks
+// across the diagonal (Knuth's delta swaps); the 64-bit shifts by 7 and 14
+// stay inside each 32-bit half, the one by 28 moves a nibble between them.
+__device__ __forceinline__ void bit_transpose8(uint32_t& lo, uint32_t& hi) {
+  uint32_t t;
+  t = (lo ^ (lo >> 7)) & 0x00AA00AAu;
+  lo ^= t ^ (t << 7);
+  t = (hi ^ (hi >> 7)) & 0x00AA00AAu;
+  hi ^= t ^ (t << 7);
+  t = (lo ^ (lo >> 14)) & 0x0000CCCCu;
+  lo ^= t ^ (t << 14);
+  t = (hi ^ (hi >> 14)) & 0x0000CCCCu;
+  hi ^= t ^ (t << 14);
+  t = (lo ^ (hi << 4)) & 0xF0F0F0F0u;
+  lo ^= t;
+  hi ^= t >> 4;
+}
+
+// The distances of one vertex to the 32 sources of a word, as bytes: q[k]
+// byte i is source 4k+i's distance, 0xFF where the visited word xs has no
+// bit. pl[b] bit j is bit b of source j's distance; unreached sources get
+// every plane bit set. Planes 0-3 and 4-7 are byte-transposed, so that word m
+// of each pair holds byte m (sources 8m..8m+7) of all eight planes, and an
+// 8x8 bit transpose of that pair turns plane-major bits into one byte per
+// source.
+template <int NPU>
+__device__ __forceinline__ void pack_distances(uint32_t xs, const uint32_t* pl, uint32_t* q) {
+  uint32_t pb[8];
+#pragma unroll
+  for (int b = 0; b < 8; ++b) pb[b] = (b < NPU ? pl[b < NPU ? b : 0] : 0u) | ~xs;
+  uint32_t lo[4], hi[4];
+  byte_transpose4(pb[0], pb[1], pb[2], pb[3], lo);
+  byte_transpose4(pb[4], pb[5], pb[6], pb[7], hi);
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    bit_transpose8(lo[m], hi[m]);
+    q[2 * m] = lo[m];
+    q[2 * m + 1] = hi[m];
+  }
+}
+
+// Byte i of w as a u32 distance, 0xFF (unreached) widened to DIST_MAX. With
+// at most 7 planes every reached distance is below 128, so one byte permute
+// that replicates the byte's sign bit does both (prmt selector nibbles with
+// bit 3 set copy the sign); with 8 planes the unreached byte is compared.
+template <int NPU>
+__device__ __forceinline__ uint32_t widen_distance(uint32_t w, uint32_t i) {
+  if constexpr (NPU <= 7) {
+    const uint32_t sel = i | ((i | 8u) << 4) | ((i | 8u) << 8) | ((i | 8u) << 12);
+    uint32_t d;
+    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(w), "r"(sel));
+    return d;
+  } else {
+    const uint32_t d = (w >> (8 * i)) & 0xFFu;
+    return d == 0xFFu ? DIST_MAX : d;
+  }
+}
+
 // Writes the rows of column cs of the staged tile: word cw = g*TW + c of the
 // 64 vertices from v0 + 64*seg, i.e. sources 32cw .. 32cw+31 of the pass.
 // Lane l owns vertices 2l and 2l+1 of the segment. NPU (planes in use) is a
 // template argument so the plane words stay in registers. Lanes flagged in
 // ovf (deeper than the planes encode) were written by the level kernel and
-// are skipped.
+// are skipped. `packed` (no ovf lane, every distance below 255) takes the
+// transposed form: each vertex's 32 distances are computed at once as bytes
+// and a row costs one byte select per vertex, against one bit extraction
+// per plane per source in the per-bit form.
 template <int W, int NPU>
 __device__ __forceinline__ void mat_column(const LevelParams& p, const MatOut& out,
                                            const uint32_t* sh, uint32_t v0, uint32_t g,
                                            uint32_t cs, uint32_t lane, uint32_t P, bool use_ovf,
-                                           bool vec_ok) {
+                                           bool packed, bool vec_ok) {
   using G = MatGeo<W>;
   const uint32_t V = p.V;
   const uint32_t c = cs % G::TW;
@@ -1082,6 +1155,47 @@ __device__ __forceinline__ void mat_column(const LevelParams& p, const MatOut& o
   }
   const uint32_t s0 = cw * 32;
   const uint32_t jn = min(32u, P - s0);
+  if (packed) {
+    uint32_t q[2][8];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      uint32_t plt[NPU > 0 ? NPU : 1];
+#pragma unroll
+      for (int b = 0; b < NPU; ++b) plt[b] = pl[b][t];
+      pack_distances<NPU>(xs[t], plt, q[t]);
+    }
+    const bool full = vec_ok && vl + 1 < V;
+    if (out.dist8) {
+      uint8_t* row = out.dist8 + (size_t)s0 * V + vl;
+#pragma unroll
+      for (uint32_t j = 0; j < 32; ++j, row += V) {
+        if (j >= jn) break;
+        const uint32_t i = j & 3;
+        const uint32_t two = __byte_perm(q[0][j >> 2], q[1][j >> 2], i | ((4 + i) << 4));
+        if (full) {
+          *reinterpret_cast<uint16_t*>(row) = (uint16_t)two;
+        } else {
+          if (vl < V) row[0] = (uint8_t)two;
+          if (vl + 1 < V) row[1] = (uint8_t)(two >> 8);
+        }
+      }
+    } else {
+      uint32_t* row = out.dist + (size_t)s0 * V + vl;
+#pragma unroll
+      for (uint32_t j = 0; j < 32; ++j, row += V) {
+        if (j >= jn) break;
+        const uint32_t d0 = widen_distance<NPU>(q[0][j >> 2], j & 3);
+        const uint32_t d1 = widen_distance<NPU>(q[1][j >> 2], j & 3);
+        if (full) {
+          *reinterpret_cast<uint2*>(row) = make_uint2(d0, d1);
+        } else {
+          if (vl < V) row[0] = d0;
+          if (vl + 1 < V) row[1] = d1;
+        }
+      }
+    }
+    return;
+  }
   if (out.dist8) {
     // Byte rows: no lane is deeper than the planes here (every distance is
     // below 255), so there is no ovf lane to skip.
@@ -1281,6 +1395,8 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS)
   const uint32_t dmax = p.ctl->level;
   const uint32_t npu = min(min(p.NP, bit_length(dmax)), (uint32_t)MAT_NPMAX);
   const bool use_ovf = dmax >= (1u << p.NP);
+  // Every reached distance fits the planes and stays below the 0xFF marker.
+  const bool packed = !use_ovf && dmax < 255u;
   // Byte rows when the pass asks for them and every distance fits a byte
   // (0xFF is kept for unreachable); the control block tells the host.
   const bool narrow = dsc->dist8 && !dsc->reach && dmax < 255u;
@@ -1349,7 +1465,7 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS)
       if (cw < wlo || cw >= whi) continue;  // no sources of this launch in this word
       switch (npu) {
 #define MAT_CASE(n) \
-  case n: mat_column<W, n>(p, out, mat_sh, v0, g, cs, lane, P, use_ovf, vec_ok); break;
+  case n: mat_column<W, n>(p, out, mat_sh, v0, g, cs, lane, P, use_ovf, packed, vec_ok); break;
         MAT_CASE(0) MAT_CASE(1) MAT_CASE(2) MAT_CASE(3) MAT_CASE(4)
         MAT_CASE(5) MAT_CASE(6) MAT_CASE(7) MAT_CASE(8)
 #undef MAT_CASE
