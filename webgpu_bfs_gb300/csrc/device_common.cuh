@@ -176,6 +176,9 @@ struct LevelKernelInfo {
 // planes (the materialisation stages 1 + NP arrays in shared memory).
 bool level_kernel_info(uint32_t W, uint32_t NP, int num_sms, LevelKernelInfo* out);
 size_t materialize_smem_bytes(uint32_t W, uint32_t NP);
+// (vertex tile, word group) items of a materialisation over V vertices at
+// W words per vertex: an upper bound on what a pass of fewer sources uses.
+size_t materialize_items(uint32_t V, uint32_t W);
 void launch_init(const LevelParams& p, cudaStream_t s);
 // Launches the level kernel of direction `dir` (DIR_PUSH / DIR_PULL), or
 // both (pull, then push) when dir is DIR_BOTH; `count` picks the form that

@@ -158,6 +158,17 @@ struct msbfs_engine {
   uint32_t split = MSBFS_SPLIT;  // in-edge slice length of bottom-up steps
   uint32_t bits_div = 64;
   uint32_t sm_share = 100;  // percent of the resident grid the persistent kernels use
+#ifndef MSBFS_MAT_WAVES
+// R-MAT scale 22, S=512, materialisation ms: 1 wave (persistent) 1.82, 2
+// 1.81, 4 1.69, 8 1.65, one block per tile 1.59. Blocks of a long
+// grid-stride loop drift apart and spread their row writes over more DRAM
+// pages; a write-only kernel with the same 256-byte row segments reaches
+// 6.5 TB/s persistent at 5 blocks per SM and 7.4 TB/s in short blocks.
+#define MSBFS_MAT_WAVES 0
+#endif
+  // Materialisation grid in waves of its resident blocks (0: one block per
+  // tile); a smaller SM share keeps it persistent at that share.
+  uint32_t mat_waves = MSBFS_MAT_WAVES;
   uint32_t level_cap = 0;   // levels per pass before MSBFS_ERR_TIMEOUT (0: V + 2)
   bool host_loop = false;
   bool zero_copy = true;  // MSBFS_ZERO_COPY=0 stages host output in HBM instead
@@ -384,7 +395,13 @@ int get_workspace(msbfs_engine* eng, const msbfs_graph* g, uint32_t W, uint32_t 
   w->count = eng->profiling == 1 || eng->profiling == 2;
   for (int d = 0; d < 2; ++d)
     w->k.level_grids[d] = std::max(1, (int)((uint64_t)w->k.level_grids[d] * eng->sm_share / 100));
-  w->k.mat_grid = std::max(1, (int)((uint64_t)w->k.mat_grid * eng->sm_share / 100));
+  if (eng->sm_share < 100) {
+    w->k.mat_grid = std::max(1, (int)((uint64_t)w->k.mat_grid * eng->sm_share / 100));
+  } else {
+    const size_t items = materialize_items((uint32_t)g->V, W);
+    const size_t want = eng->mat_waves ? (size_t)w->k.mat_grid * eng->mat_waves : items;
+    w->k.mat_grid = (int)std::max<size_t>(1, std::min(want, items));
+  }
   w->k.red_grid = std::max(1, (int)((uint64_t)w->k.red_grid * eng->sm_share / 100));
   LevelParams& p = w->p;
   p.V = (uint32_t)g->V;
@@ -1186,6 +1203,8 @@ int msbfs_engine_create(int device, int method, msbfs_engine** out) {
   e->zero_copy = !(zc && zc[0] == '0');
   const char* nr = getenv("MSBFS_NARROW");
   e->narrow = !(nr && nr[0] == '0');
+  const char* mw = getenv("MSBFS_MAT_WAVES");
+  if (mw) e->mat_waves = (uint32_t)std::max(0, atoi(mw));
   const char* sr = getenv("MSBFS_SPLIT_ROWS");
   if (sr) e->split_frac = std::min(1.0, std::max(0.0, atof(sr)));
   *out = eng.release();

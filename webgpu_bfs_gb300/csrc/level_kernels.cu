@@ -1378,6 +1378,67 @@ __global__ void __launch_bounds__(RED_BLOCK, RED_MIN_BLOCKS) reduce_kernel(Level
   }
 }
 
+// Stages arrays A0..A1 of one tile (array 0 is the visited words, array
+// a > 0 plane a - 1): this thread's four words of each, transposed into
+// shared memory ([word][vertex] per array), zeroing in global memory the
+// words that were not zero when `clear` is set. All loads of the range are
+// issued before the first shared store so that their latencies overlap.
+template <int W, int A0, int A1>
+__device__ __forceinline__ void stage_arrays(const LevelParams& p, uint32_t* sh, size_t gw,
+                                             bool inb, bool vec_planes, bool clear, uint32_t o) {
+  using G = MatGeo<W>;
+  constexpr int N = A1 - A0 + 1;
+  const size_t VW = (size_t)p.V * W;
+  uint32_t x[N][4];
+  bool vec[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const int a = A0 + i;
+    const uint32_t* src = a == 0 ? p.vis : p.planes + (size_t)(a - 1) * VW;
+    vec[i] = inb && (a == 0 || vec_planes);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x[i][k] = 0;
+    if (vec[i]) {
+      const uint4 t = *reinterpret_cast<const uint4*>(src + gw);
+      x[i][0] = t.x;
+      x[i][1] = t.y;
+      x[i][2] = t.z;
+      x[i][3] = t.w;
+    } else if constexpr (W <= 16) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (gw + k < VW) x[i][k] = src[gw + k];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const int a = A0 + i;
+    uint32_t* src = a == 0 ? p.vis : p.planes + (size_t)(a - 1) * VW;
+    if (clear) {
+      if (vec[i]) {
+        if (x[i][0] | x[i][1] | x[i][2] | x[i][3])
+          *reinterpret_cast<uint4*>(src + gw) = make_uint4(0, 0, 0, 0);
+      } else if constexpr (W <= 16) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (gw + k < VW && x[i][k]) src[gw + k] = 0;
+      }
+    }
+    uint32_t* dst = sh + a * G::ARR;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) dst[((o + k) % G::TW) * G::RS + (o + k) / G::TW] = x[i][k];
+  }
+}
+
+// Stages the visited words and the NPU planes in use of one tile, at most
+// five arrays in flight at a time (the register budget of 5 blocks per SM).
+template <int W, int NPU>
+__device__ __forceinline__ void stage_tile(const LevelParams& p, uint32_t* sh, size_t gw,
+                                           bool inb, bool vec_planes, bool clear, uint32_t o) {
+  stage_arrays<W, 0, (NPU < 4 ? NPU : 4)>(p, sh, gw, inb, vec_planes, clear, o);
+  if constexpr (NPU > 4) stage_arrays<W, 5, NPU>(p, sh, gw, inb, vec_planes, clear, o);
+}
+
 // Turns visited words + level planes into the source-major u32 distance rows
 // (or copies the visited words out as a reachability bitmask) and zeroes the
 // words it read, so the next pass starts from clean buffers. Blocks take
@@ -1439,25 +1500,13 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS)
       gw = (size_t)(v0 + o / 16) * W + 16 * g + (o % 16);
       inb = v0 + o / 16 < V;
     }
-    for (uint32_t a = 0; a <= npu; ++a) {
-      uint32_t* src = a == 0 ? p.vis : p.planes + (size_t)(a - 1) * VW;
-      uint32_t x[4] = {0, 0, 0, 0};
-      if (inb && (a == 0 || vec_planes)) {
-        const uint4 t = *reinterpret_cast<const uint4*>(src + gw);
-        x[0] = t.x; x[1] = t.y; x[2] = t.z; x[3] = t.w;
-        if (clear && (t.x | t.y | t.z | t.w))
-          *reinterpret_cast<uint4*>(src + gw) = make_uint4(0, 0, 0, 0);
-      } else if constexpr (W <= 16) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (gw + k < VW) {
-            x[k] = src[gw + k];
-            if (clear && x[k]) src[gw + k] = 0;
-          }
-      }
-      uint32_t* dst = mat_sh + a * G::ARR;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) dst[((o + k) % G::TW) * G::RS + (o + k) / G::TW] = x[k];
+    switch (npu) {
+#define STAGE_CASE(n) \
+  case n: stage_tile<W, n>(p, mat_sh, gw, inb, vec_planes, clear, o); break;
+      STAGE_CASE(0) STAGE_CASE(1) STAGE_CASE(2) STAGE_CASE(3) STAGE_CASE(4)
+      STAGE_CASE(5) STAGE_CASE(6) STAGE_CASE(7) STAGE_CASE(8)
+#undef STAGE_CASE
+      default: break;
     }
     __syncthreads();
     for (uint32_t cs = warp; cs < MAT_COLS; cs += MAT_BLOCK / 32) {
@@ -1474,6 +1523,12 @@ __global__ void __launch_bounds__(MAT_BLOCK, MAT_MIN_BLOCKS)
     }
     __syncthreads();
   }
+}
+
+size_t materialize_items(uint32_t V, uint32_t W) {
+  const uint32_t tw = W <= 16 ? W : 16;
+  const uint32_t tv = MAT_TILE_WORDS / tw;
+  return (size_t)((V + tv - 1) / tv) * ((W + tw - 1) / tw);
 }
 
 size_t materialize_smem_bytes(uint32_t W, uint32_t NP) {
