@@ -118,6 +118,39 @@ __device__ __forceinline__ Words<VEC> ldg_words(const uint32_t* p) {
   return r;
 }
 
+// Frontier-row gathers of the bottom-up step (random rows, L1 hit rate
+// 14-21% on R-MAT 22). MSBFS_GATHER_LOAD picks the cache path: 0 the
+// read-only path, 1 the same without allocating in L1, 2 L2 only. R-MAT
+// scale 22, S=512, step ms: 7.54 / 8.03 / 7.63 -- the hubs' rows that L1
+// keeps are worth its allocation traffic.
+#ifndef MSBFS_GATHER_LOAD
+#define MSBFS_GATHER_LOAD 0
+#endif
+template <int VEC>
+__device__ __forceinline__ Words<VEC> gather_words(const uint32_t* p) {
+  if constexpr (MSBFS_GATHER_LOAD == 1 && VEC == 4) {
+    Words<VEC> r;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.w[0]), "=r"(r.w[1]), "=r"(r.w[2]), "=r"(r.w[3])
+                 : "l"(p));
+    return r;
+  } else if constexpr (MSBFS_GATHER_LOAD == 2) {
+    Words<VEC> r;
+    if constexpr (VEC == 4) {
+      uint4 t = __ldcg(reinterpret_cast<const uint4*>(p));
+      r.w[0] = t.x; r.w[1] = t.y; r.w[2] = t.z; r.w[3] = t.w;
+    } else if constexpr (VEC == 2) {
+      uint2 t = __ldcg(reinterpret_cast<const uint2*>(p));
+      r.w[0] = t.x; r.w[1] = t.y;
+    } else {
+      r.w[0] = __ldcg(p);
+    }
+    return r;
+  } else {
+    return ldg_words<VEC>(p);
+  }
+}
+
 // L2-coherent read of words other blocks update with atomics this level.
 template <int VEC>
 __device__ __forceinline__ Words<VEC> ldcg_words(const uint32_t* p) {
@@ -478,7 +511,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         for (int j = 0; j < CH; ++j) {
           if (u[j] != FULL) {
             cnt.rows += 1;
-            Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
+            Words<VEC> f = gather_words<VEC>(Fin + (size_t)u[j] * W + k0);
 #pragma unroll
             for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
           }
@@ -609,7 +642,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         for (int j = 0; j < CH; ++j) {
           if (!lane_sat && u[j] != FULL) {
             cnt.rows += 1;
-            f[j] = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
+            f[j] = gather_words<VEC>(Fin + (size_t)u[j] * W + k0);
           } else {
 #pragma unroll
             for (int q = 0; q < VEC; ++q) f[j].w[q] = 0;
@@ -669,7 +702,7 @@ __device__ void pull_phase(const LevelParams& p, BlockQueue& bq, uint32_t* s_lan
         for (int j = 0; j < CH; ++j) {
           if (u[j] != FULL) {
             cnt.rows += 1;
-            Words<VEC> f = ldg_words<VEC>(Fin + (size_t)u[j] * W + k0);
+            Words<VEC> f = gather_words<VEC>(Fin + (size_t)u[j] * W + k0);
 #pragma unroll
             for (int q = 0; q < VEC; ++q) hc.w[q] |= f.w[q];
           }
