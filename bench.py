@@ -30,6 +30,15 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+SERVED_SIZES = (1, 8, 64, 512, 2048)
+SERVED_CONFIG = dict(slots=4, express_slots=1, small_sources=64, general_sm_percent=85,
+                     max_sources_per_launch=512)
+# The mixed {1, 8, 64, 512, 2048} stream: general slots pack up to 2,048
+# lanes into one 64-word pass (two of them: ~52 GB of traversal state each
+# on R-MAT scale 24), the express slot takes requests of <= 64 sources.
+SERVED_CONFIG_WIDE = dict(slots=3, express_slots=1, small_sources=64, general_sm_percent=85,
+                          max_sources_per_launch=2048)
+
 WORKLOADS = {
     # name: generator spec, sources, seed
     "rmat22_s512": dict(kind="rmat", scale=22, ef=16, S=512, seed=20220),
@@ -43,7 +52,8 @@ WORKLOADS = {
     # served form: a resident graph answering a Poisson stream of requests
     # with |S| drawn from {1, 8, 64, 512, 2048}, per-source statistics out
     "served_rmat24": dict(kind="served", graph=dict(kind="rmat", scale=24, ef=16, seed=24024),
-                          requests=160, seed=5150, verify_sources=48),
+                          requests=160, seed=5150, verify_sources=48,
+                          server=SERVED_CONFIG_WIDE),
     "served_road1448": dict(kind="served",
                             graph=dict(kind="road", w=1448, h=1448, extra=41934, seed=1448),
                             requests=240, seed=5151),
@@ -58,9 +68,6 @@ WORKLOADS = {
                                             general_sm_percent=100,
                                             max_sources_per_launch=512)),
 }
-SERVED_SIZES = (1, 8, 64, 512, 2048)
-SERVED_CONFIG = dict(slots=4, express_slots=1, small_sources=64, general_sm_percent=85,
-                     max_sources_per_launch=512)
 L2_BYTES = 129 * 2**20
 
 

@@ -319,7 +319,9 @@ int msbfs_run_ms_bfs_stats(msbfs_engine *engine, const msbfs_graph *graph,
 typedef struct msbfs_server msbfs_server;
 typedef struct msbfs_server_config {
   uint32_t slots;                  /* traversals in flight (0 -> 2)            */
-  uint32_t max_sources_per_launch; /* lanes packed per launch (0 -> 512)       */
+  uint32_t max_sources_per_launch; /* lanes packed per launch (0 -> 512); above
+                                      512, general slots run each launch as one
+                                      pass of up to 64 words (2,048 lanes)    */
   uint64_t hbm_budget_bytes;       /* row pool of all slots (0 -> 8 GiB)       */
   int method;                      /* engine method (MSBFS_METHOD_AUTO)        */
   uint32_t express_slots;          /* slots reserved for small requests (0)    */
