@@ -29,14 +29,27 @@ namespace msbfs {
 
 constexpr uint32_t CTA_DIST_MAX = 0xffffffffu;
 constexpr int CTA_THREADS = 512;
-// Two register budgets per kernel: MINB = 3 resident blocks per SM (40
-// registers: 4 edge records in flight, the shortest level latency) and MINB =
-// 4 (32 registers, 2 records in flight, every thread slot of the SM). A call
-// with more sources than 3 blocks per SM can hold gets the 4-block form:
-// many-source calls are bound by how many BFSs run at once, single ones by
-// the per-level latency chain.
+// Two forms. The latency form: blocks of 512 threads, 3 resident per SM (40
+// registers: 4 edge records in flight, the shortest level latency). The
+// throughput form, for calls with more sources than 3 blocks per SM can
+// hold: CTA_TPUT_THREADS threads and CTA_TPUT_MINB resident blocks per SM
+// (2 records in flight): many-source calls are bound by how many BFSs run
+// at once, single ones by the per-level latency chain.
 constexpr int CTA_MINB_LATENCY = 3;
-constexpr int CTA_MINB_THROUGHPUT = 4;
+// Road 339x338 + 5,000 edges, S=2048 (threads x blocks per SM, ms): 512 x 4
+// 5.41, 384 x 5 4.92, 256 x 6 5.16, 256 x 7 4.46, 256 x 8 4.78, 128 x 12
+// 6.68, 128 x 16 6.78. Each block waits at one barrier per level while a
+// few of its warps walk a frontier of a few hundred vertices: smaller blocks
+// put more sources in flight, until too few threads share a level's work.
+#ifndef MSBFS_CTA_TPUT_THREADS
+#define MSBFS_CTA_TPUT_THREADS 256
+#endif
+#ifndef MSBFS_CTA_TPUT_MINB
+#define MSBFS_CTA_TPUT_MINB 7
+#endif
+constexpr int CTA_TPUT_THREADS = MSBFS_CTA_TPUT_THREADS;
+constexpr int CTA_MINB_THROUGHPUT = MSBFS_CTA_TPUT_MINB;
+static_assert(CTA_MINB_THROUGHPUT > CTA_MINB_LATENCY, "the throughput form holds more blocks");
 // Global-bitmap mode keeps its per-block scratch (queue slab + bitmap) within
 // this many bytes by shrinking the grid.
 constexpr size_t CTA_GLOBAL_SCRATCH_BYTES = 4ull << 30;
@@ -74,8 +87,8 @@ constexpr int CTA_CLUSTER_ER_BATCH = MSBFS_CTA_CLUSTER_ER_BATCH;
 // Counters: level L appends through s_cnt[L % 3]; thread 0 clears
 // s_cnt[(L+1) % 3] during level L (last read right after the barrier of
 // level L-2), so a level needs one block barrier.
-template <bool GB, bool ER, int MINB>
-__global__ void __launch_bounds__(CTA_THREADS, MINB) cta_bfs_kernel(CtaParams p) {
+template <bool GB, bool ER, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) cta_bfs_kernel(CtaParams p) {
   constexpr int CTA_ER_BATCH = MINB >= CTA_MINB_THROUGHPUT ? 2 : 4;
   extern __shared__ __align__(16) uint32_t smem_dyn[];
   __shared__ uint32_t s_src_idx;
@@ -396,19 +409,20 @@ size_t cta_max_vertices(int device) {
   return ((size_t)optin - reserve) * 8;
 }
 
-template <bool GB, bool ER, int MINB>
+template <bool GB, bool ER, int THREADS, int MINB>
 static int cta_occupancy(int block, size_t smem) {
-  cudaFuncSetAttribute(cta_bfs_kernel<GB, ER, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
+  auto fn = cta_bfs_kernel<GB, ER, THREADS, MINB>;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cta_bfs_kernel<GB, ER, MINB>, block, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, smem);
   return occ;
 }
 
 template <bool GB, bool ER>
 static int cta_occupancy(int minb, int block, size_t smem) {
-  return minb >= CTA_MINB_THROUGHPUT ? cta_occupancy<GB, ER, CTA_MINB_THROUGHPUT>(block, smem)
-                                     : cta_occupancy<GB, ER, CTA_MINB_LATENCY>(block, smem);
+  return minb >= CTA_MINB_THROUGHPUT
+             ? cta_occupancy<GB, ER, CTA_TPUT_THREADS, CTA_MINB_THROUGHPUT>(block, smem)
+             : cta_occupancy<GB, ER, CTA_THREADS, CTA_MINB_LATENCY>(block, smem);
 }
 
 template <int CL, bool ER>
@@ -506,11 +520,11 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_recor
   if (!shared_bits && cta_cluster_shape(V, sms, optin, edge_records, num_sources, out))
     return true;
   CtaShape sh{};
-  sh.block = CTA_THREADS;
   sh.edge_records = edge_records;
   sh.global_bits = !shared_bits;
   sh.minb = (shared_bits && num_sources > (size_t)sms * CTA_MINB_LATENCY) ? CTA_MINB_THROUGHPUT
                                                                           : CTA_MINB_LATENCY;
+  sh.block = sh.minb >= CTA_MINB_THROUGHPUT ? CTA_TPUT_THREADS : CTA_THREADS;
   // The queue halves get the shared memory left once the bitmaps of minb
   // resident blocks have theirs, so the queue never costs a resident block.
   // A frontier beyond the halves continues in the global slab.
@@ -543,9 +557,10 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_recor
 template <bool GB, bool ER>
 static void launch_cta_t(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s) {
   if (sh.minb >= CTA_MINB_THROUGHPUT)
-    cta_bfs_kernel<GB, ER, CTA_MINB_THROUGHPUT><<<grid, sh.block, sh.smem, s>>>(p);
+    cta_bfs_kernel<GB, ER, CTA_TPUT_THREADS, CTA_MINB_THROUGHPUT>
+        <<<grid, sh.block, sh.smem, s>>>(p);
   else
-    cta_bfs_kernel<GB, ER, CTA_MINB_LATENCY><<<grid, sh.block, sh.smem, s>>>(p);
+    cta_bfs_kernel<GB, ER, CTA_THREADS, CTA_MINB_LATENCY><<<grid, sh.block, sh.smem, s>>>(p);
 }
 
 void launch_cta(const CtaParams& params, const CtaShape& sh, int grid, cudaStream_t s) {
