@@ -63,9 +63,13 @@ def _requests(rng, V, n):
     return out
 
 
-@pytest.mark.parametrize("graph_kind,express", [("rmat", 0), ("road", 0), ("rmat", 1),
-                                                ("road", 1)])
-def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind, express):
+@pytest.mark.parametrize("graph_kind,express,lanes", [("rmat", 0, 512), ("road", 0, 512),
+                                                      ("rmat", 1, 512), ("road", 1, 512),
+                                                      ("rmat", 1, 2048)])
+def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind, express, lanes):
+    """Mixed requests from two threads equal the same requests alone and the
+    oracle. With 2,048 lanes per launch the general slots run each launch as
+    one pass of up to 64 words per vertex."""
     torch = pytest.importorskip("torch")
     if graph_kind == "rmat":
         g = native.generate_graph500_rmat(12, 8, 71)
@@ -75,7 +79,7 @@ def test_server_mix_equals_alone_equals_oracle(native, oracle, graph_kind, expre
     rng = np.random.default_rng(3 + express)
     reqs = _requests(rng, V, 14)
     slots = 2 + express
-    srv = native.BfsServer(g, slots=slots, max_sources_per_launch=512,
+    srv = native.BfsServer(g, slots=slots, max_sources_per_launch=lanes,
                            hbm_budget_bytes=slots * 300 * V * 4,  # forces row splitting
                            express_slots=express, small_sources=8,
                            general_sm_percent=70 if express else 100)
