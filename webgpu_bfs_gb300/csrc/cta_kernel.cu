@@ -28,9 +28,20 @@ namespace cg = cooperative_groups;
 namespace msbfs {
 
 constexpr uint32_t CTA_DIST_MAX = 0xffffffffu;
-constexpr int CTA_THREADS = 512;
-// Two forms. The latency form: blocks of 512 threads, 3 resident per SM (40
-// registers: 4 edge records in flight, the shortest level latency). The
+// Latency form's block (ms; road 339x338 + 5,000 edges S=256 / S=1, grid
+// 64x64 S=64): 512 threads 1.216 / 0.964 / 0.123, 256 threads 1.148 /
+// 0.912 / 0.109, 128 threads 1.402 / 1.275 / 0.109. A level of a few
+// hundred frontier vertices keeps 256 threads busy, and a smaller block's
+// barrier costs less.
+#ifndef MSBFS_CTA_LAT_THREADS
+#define MSBFS_CTA_LAT_THREADS 256
+#endif
+constexpr int CTA_THREADS = MSBFS_CTA_LAT_THREADS;
+// Global-bitmap mode (graphs whose bitmap does not fit shared memory, e.g.
+// road 1448 x 1448) keeps 512-thread blocks: its frontiers are wider.
+constexpr int CTA_GB_THREADS = 512;
+// Two forms. The latency form: blocks of CTA_THREADS threads, 3 resident
+// per SM (4 edge records in flight, the shortest level latency). The
 // throughput form, for calls with more sources than 3 blocks per SM can
 // hold: CTA_TPUT_THREADS threads and CTA_TPUT_MINB resident blocks per SM
 // (2 records in flight): many-source calls are bound by how many BFSs run
@@ -420,9 +431,10 @@ static int cta_occupancy(int block, size_t smem) {
 
 template <bool GB, bool ER>
 static int cta_occupancy(int minb, int block, size_t smem) {
+  constexpr int LT = GB ? CTA_GB_THREADS : CTA_THREADS;
   return minb >= CTA_MINB_THROUGHPUT
              ? cta_occupancy<GB, ER, CTA_TPUT_THREADS, CTA_MINB_THROUGHPUT>(block, smem)
-             : cta_occupancy<GB, ER, CTA_THREADS, CTA_MINB_LATENCY>(block, smem);
+             : cta_occupancy<GB, ER, LT, CTA_MINB_LATENCY>(block, smem);
 }
 
 template <int CL, bool ER>
@@ -524,7 +536,9 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_recor
   sh.global_bits = !shared_bits;
   sh.minb = (shared_bits && num_sources > (size_t)sms * CTA_MINB_LATENCY) ? CTA_MINB_THROUGHPUT
                                                                           : CTA_MINB_LATENCY;
-  sh.block = sh.minb >= CTA_MINB_THROUGHPUT ? CTA_TPUT_THREADS : CTA_THREADS;
+  sh.block = sh.minb >= CTA_MINB_THROUGHPUT ? CTA_TPUT_THREADS
+             : shared_bits                    ? CTA_THREADS
+                                              : CTA_GB_THREADS;
   // The queue halves get the shared memory left once the bitmaps of minb
   // resident blocks have theirs, so the queue never costs a resident block.
   // A frontier beyond the halves continues in the global slab.
@@ -556,11 +570,12 @@ bool cta_launch_shape(uint32_t V, int device, bool allow_global, bool edge_recor
 
 template <bool GB, bool ER>
 static void launch_cta_t(const CtaParams& p, const CtaShape& sh, int grid, cudaStream_t s) {
+  constexpr int LT = GB ? CTA_GB_THREADS : CTA_THREADS;
   if (sh.minb >= CTA_MINB_THROUGHPUT)
     cta_bfs_kernel<GB, ER, CTA_TPUT_THREADS, CTA_MINB_THROUGHPUT>
         <<<grid, sh.block, sh.smem, s>>>(p);
   else
-    cta_bfs_kernel<GB, ER, CTA_THREADS, CTA_MINB_LATENCY><<<grid, sh.block, sh.smem, s>>>(p);
+    cta_bfs_kernel<GB, ER, LT, CTA_MINB_LATENCY><<<grid, sh.block, sh.smem, s>>>(p);
 }
 
 void launch_cta(const CtaParams& params, const CtaShape& sh, int grid, cudaStream_t s) {
