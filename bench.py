@@ -60,6 +60,9 @@ WORKLOADS = {
     # requests of at most 64 sources only, on the R-MAT scale 22 graph: the
     # request size the p99 <= 20 ms target is stated for; every slot packs
     # up to 512 lanes (no express split: all requests are small)
+    # Matrix Market reader (host only): R-MAT scale 20 written as a symmetric
+    # pattern file, parsed by all host threads and by one
+    "mtx_rmat20": dict(kind="mtx", graph=dict(kind="rmat", scale=20, ef=16, seed=2020)),
     "served_rmat22_small": dict(kind="served",
                                 graph=dict(kind="rmat", scale=22, ef=16, seed=20220),
                                 requests=400, seed=5152, sizes=(1, 8, 64), verify_sources=128,
@@ -1062,6 +1065,72 @@ def run_ncu_case(args, spec):
     eng.close()
 
 
+def mtx_text(g):
+    """A symmetric graph as Matrix Market text: a pattern-symmetric banner and
+    its lower triangle (row > column), 1-based."""
+    V = g.num_vertices
+    off = g.row_offsets.astype(np.int64)
+    rows = np.repeat(np.arange(V, dtype=np.int64), np.diff(off))
+    cols = g.col_indices.astype(np.int64)
+    keep = rows > cols
+    r, c = rows[keep] + 1, cols[keep] + 1
+    lines = "\n".join(f"{a} {b}" for a, b in zip(r.tolist(), c.tolist()))
+    head = f"%%MatrixMarket matrix coordinate pattern symmetric\n% generated\n{V} {V} {r.size}\n"
+    return (head + lines + "\n").encode(), int(r.size)
+
+
+def run_mtx(args, spec):
+    """Times the Matrix Market reader (MtxReader::parse, crates/core/src/mtx.rs)
+    on generated text with every host thread and with one, and checks that
+    the parsed graph is the generated one."""
+    import __graft_entry__
+    __graft_entry__.build()
+    import webgpu_bfs_gb300 as m
+    g = make_graph(m, spec["graph"])
+    t0 = time.perf_counter()
+    text, entries = mtx_text(g)
+    gen_s = time.perf_counter() - t0
+    steps = max(1, args.steps)
+
+    def timed(threads):
+        if threads:
+            os.environ["MSBFS_HOST_THREADS"] = str(threads)
+        else:
+            os.environ.pop("MSBFS_HOST_THREADS", None)
+        parsed = m.parse_mtx(text)  # warm
+        ts = []
+        for _ in range(steps):
+            t = time.perf_counter()
+            parsed = m.parse_mtx(text)
+            ts.append(time.perf_counter() - t)
+        os.environ.pop("MSBFS_HOST_THREADS", None)
+        return parsed, float(np.median(ts))
+
+    parsed, t_all = timed(0)
+    _, t_one = timed(1)
+    same = (parsed.num_vertices == g.num_vertices and
+            np.array_equal(parsed.row_offsets, g.row_offsets) and
+            np.array_equal(parsed.col_indices, g.col_indices))
+    res = {
+        "metric": "Matrix Market parse entries/s", "value": entries / t_all,
+        "unit": "entries/s", "n_gpus": 0, "steps": steps, "warmup": 1,
+        "ms_per_step": 1000 * t_all, "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "text", "data": "synthetic",
+        "config": {"workload": args.workload, "graph": spec["graph"],
+                   "num_vertices": g.num_vertices, "stored_edges": g.num_edges,
+                   "entries": entries, "text_mb": round(len(text) / 1e6, 1),
+                   "threads": os.cpu_count(), "cpu_model": cpu_model(),
+                   "generation_s": round(gen_s, 1)},
+        "mb_per_s": len(text) / t_all / 1e6,
+        "single_thread": {"value": entries / t_one, "unit": "entries/s",
+                          "ms_per_step": 1000 * t_one, "mb_per_s": len(text) / t_one / 1e6},
+        "parity": {"parsed_equals_generated": bool(same)},
+    }
+    print(json.dumps(res), flush=True)
+    if not same:
+        sys.exit(3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1093,6 +1162,8 @@ def main():
         run_batched(args, spec)
     elif spec["kind"] == "served" and args.impl != "reference":
         run_served(args, spec)
+    elif spec["kind"] == "mtx":
+        run_mtx(args, spec)
     elif args.impl == "reference":
         run_reference(args, spec)
     else:

@@ -163,3 +163,23 @@ def test_read_file(native, tmp_path):
     with pytest.raises(native.MtxError) as e:
         native.read_mtx(tmp_path / "missing.mtx")
     assert e.value.kind == "Io"
+
+
+@pytest.mark.parametrize("threads", ["1", "3", None])
+def test_host_thread_counts_give_the_generated_graph(native, monkeypatch, threads):
+    """A generated R-MAT graph written as a symmetric pattern file (its lower
+    triangle) parses back to the same CSR whatever the number of host threads
+    (MSBFS_HOST_THREADS): the entries are split into per-thread chunks and the
+    CSR is built from source-vertex partitions, both sized by the count."""
+    import bench
+    if threads:
+        monkeypatch.setenv("MSBFS_HOST_THREADS", threads)
+    else:
+        monkeypatch.delenv("MSBFS_HOST_THREADS", raising=False)
+    g = native.generate_graph500_rmat(15, 16, 5)
+    text, entries = bench.mtx_text(g)
+    assert entries * 2 == g.num_edges and len(text) > 3 << 20  # several 1 MB chunks
+    p = native.parse_mtx(text)
+    assert p.num_vertices == g.num_vertices
+    assert np.array_equal(p.row_offsets, g.row_offsets)
+    assert np.array_equal(p.col_indices, g.col_indices)

@@ -10,12 +10,19 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <cstdlib>
 #include <thread>
 
 namespace msbfs {
 
 int host_threads() {
   unsigned n = std::thread::hardware_concurrency();
+  // MSBFS_HOST_THREADS caps the host-side parallel work (graph building,
+  // the Matrix Market reader) for processes that share the host's cores.
+  if (const char* e = getenv("MSBFS_HOST_THREADS")) {
+    const int v = atoi(e);
+    if (v > 0) n = (unsigned)v;
+  }
   if (n == 0) n = 1;
   if (n > 64) n = 64;
   return (int)n;
@@ -112,6 +119,115 @@ HostCsr csr_from_pairs(size_t V, const std::vector<uint64_t>& pairs, bool symmet
     }
   });
   // 4. compact
+  for (size_t i = 0; i < V; ++i) g.off[i + 1] = g.off[i] + cnt[i];
+  g.E = g.off[V];
+  g.idx.resize(g.E);
+  parallel_dynamic(V, 4096, [&](size_t b, size_t e) {
+    for (size_t x = b; x < e; ++x)
+      if (cnt[x])
+        std::memcpy(g.idx.data() + g.off[x], raw.data() + raw_off[x], cnt[x] * sizeof(uint32_t));
+  });
+  return g;
+}
+
+HostCsr csr_from_pair_lists(size_t V, const std::vector<const std::vector<uint64_t>*>& lists) {
+  HostCsr g;
+  g.V = V;
+  g.off.assign(V + 1, 0);
+  if (V == 0) return g;
+  const int T = host_threads();
+  // Slices of the input lists, the unit of the two parallel passes below.
+  struct Slice {
+    const uint64_t* p;
+    size_t n;
+  };
+  size_t n = 0;
+  for (const auto* l : lists) n += l->size();
+  const size_t piece = std::max<size_t>(size_t(1) << 16, (n + 4 * (size_t)T - 1) / (4 * (size_t)T));
+  std::vector<Slice> slices;
+  for (const auto* l : lists)
+    for (size_t b = 0; b < l->size(); b += piece)
+      slices.push_back(Slice{l->data() + b, std::min(piece, l->size() - b)});
+  // Partitions: P = 2^pbits contiguous source ranges of 2^shift vertices.
+  unsigned bits = 0;
+  while ((size_t(1) << bits) < V) ++bits;
+  unsigned pbits = 0;
+  while ((size_t(1) << pbits) < 8 * (size_t)T && pbits < bits) ++pbits;
+  const unsigned shift = bits - pbits;
+  const size_t P = size_t(1) << pbits;
+  const size_t S = slices.size();
+  auto valid = [V](uint64_t x) {
+    const uint32_t a = (uint32_t)(x >> 32), c = (uint32_t)x;
+    return a != c && a < V && c < V;
+  };
+  // 1. per-slice histogram of partitions
+  std::vector<uint64_t> hist(S * P, 0);
+  parallel_dynamic(S, 1, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      uint64_t* h = hist.data() + i * P;
+      for (size_t k = 0; k < slices[i].n; ++k) {
+        const uint64_t x = slices[i].p[k];
+        if (valid(x)) ++h[(x >> 32) >> shift];
+      }
+    }
+  });
+  // 2. write cursors, partition-major then slice: each partition's pairs
+  // end up contiguous in `part`
+  std::vector<uint64_t> pbase(P + 1, 0);
+  uint64_t m = 0;
+  for (size_t q = 0; q < P; ++q) {
+    pbase[q] = m;
+    for (size_t i = 0; i < S; ++i) {
+      const uint64_t c = hist[i * P + q];
+      hist[i * P + q] = m;
+      m += c;
+    }
+  }
+  pbase[P] = m;
+  std::vector<uint64_t> part(m ? m : 1);
+  parallel_dynamic(S, 1, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      uint64_t* h = hist.data() + i * P;
+      for (size_t k = 0; k < slices[i].n; ++k) {
+        const uint64_t x = slices[i].p[k];
+        if (valid(x)) part[h[(x >> 32) >> shift]++] = x;
+      }
+    }
+  });
+  // 3. each partition: degrees, offsets and targets of its own vertices
+  std::vector<uint32_t> raw(m ? m : 1);
+  std::vector<uint64_t> raw_off(V + 1, 0);
+  raw_off[V] = m;
+  parallel_dynamic(P, 1, [&](size_t b, size_t e) {
+    std::vector<uint32_t> cur;
+    for (size_t q = b; q < e; ++q) {
+      const size_t lo = q << shift, hi = std::min(V, (q + 1) << shift);
+      if (lo >= hi) continue;
+      cur.assign(hi - lo, 0);
+      for (uint64_t k = pbase[q]; k < pbase[q + 1]; ++k) ++cur[(part[k] >> 32) - lo];
+      uint64_t run = pbase[q];
+      for (size_t u = lo; u < hi; ++u) {
+        raw_off[u] = run;
+        run += cur[u - lo];
+        cur[u - lo] = 0;
+      }
+      for (uint64_t k = pbase[q]; k < pbase[q + 1]; ++k) {
+        const size_t u = (size_t)(part[k] >> 32);
+        raw[raw_off[u] + cur[u - lo]++] = (uint32_t)part[k];
+      }
+    }
+  });
+  std::vector<uint64_t>().swap(part);
+  // 4. per-vertex sort + dedup, 5. compact (as csr_from_pairs)
+  std::vector<uint32_t> cnt(V, 0);
+  parallel_dynamic(V, 4096, [&](size_t b, size_t e) {
+    for (size_t x = b; x < e; ++x) {
+      uint32_t* lo = raw.data() + raw_off[x];
+      uint32_t* hi = raw.data() + raw_off[x + 1];
+      std::sort(lo, hi);
+      cnt[x] = (uint32_t)(std::unique(lo, hi) - lo);
+    }
+  });
   for (size_t i = 0; i < V; ++i) g.off[i + 1] = g.off[i] + cnt[i];
   g.E = g.off[V];
   g.idx.resize(g.E);

@@ -44,6 +44,11 @@ HostCsr csr_from_edge_list(size_t V, const uint32_t* u, const uint32_t* v, size_
 // parallel: per-vertex adjacency sort + dedup. `pairs` holds (u, v) packed as
 // u << 32 | v. Self-loops and out-of-range endpoints are dropped.
 HostCsr csr_from_pairs(size_t V, const std::vector<uint64_t>& pairs, bool symmetrise);
+// The same CSR from several lists of (u << 32 | v) pairs taken as one edge
+// list, without concatenating them and without atomics: the pairs are
+// radix-partitioned by source vertex range, then each range is built by one
+// thread. Needs 8 bytes of scratch per pair.
+HostCsr csr_from_pair_lists(size_t V, const std::vector<const std::vector<uint64_t>*>& lists);
 // CsrGraph::to_csc (graph.rs:90-127), counting-sort transpose.
 HostCsr transpose(size_t V, size_t E, const uint32_t* off, const uint32_t* idx);
 // CsrGraph::is_symmetric (graph.rs:129-133).

@@ -330,7 +330,6 @@ bool parse(const char* text, size_t len, msbfs::HostCsr* out, Err* err) {
     for (auto& x : th) x.join();
   }
   uint64_t base = line_no;  // lines before the entry section
-  size_t total = 0;
   for (Chunk& c : chunks) {
     if (c.failed) {
       Err e = c.err;
@@ -344,15 +343,10 @@ bool parse(const char* text, size_t len, msbfs::HostCsr* out, Err* err) {
       return false;
     }
     base += c.lines;
-    total += c.pairs.size();
   }
-  std::vector<uint64_t> pairs;
-  pairs.reserve(total);
-  for (Chunk& c : chunks) {
-    pairs.insert(pairs.end(), c.pairs.begin(), c.pairs.end());
-    std::vector<uint64_t>().swap(c.pairs);
-  }
-  *out = msbfs::csr_from_pairs((size_t)V, pairs, false);
+  std::vector<const std::vector<uint64_t>*> lists;
+  for (const Chunk& c : chunks) lists.push_back(&c.pairs);
+  *out = msbfs::csr_from_pair_lists((size_t)V, lists);
   return true;
 }
 
